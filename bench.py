@@ -1,0 +1,343 @@
+"""Throughput of the SPH2S single-scale step on GB300 (particle-steps/s).
+
+Default workload: the 2M-particle dam break (2,097,152 fluid + 2,043,880
+boundary particles, 128^3 cells, dt 2.5e-5), 100 warm-up + 1,000 timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c1|c0] [--no-cpu-baseline]
+
+`value` is device-timed (CUDA events on the solver's stream, state resident in
+HBM); `e2e` goes through the public API (sph_create from host arrays, then per
+step sph_advance + a device->host read of the positions into pinned memory).
+`--impl reference` times the CPU restatement of the reference step (the
+reference has no CPU path of its own and its CUDA 5.0/OpenGL build cannot run
+here) on the host cores.  With N > 1 each rank runs an independent replica
+(the path does not shard; there is no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s"
+UNIT = "particle-steps/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["c1", "c0"], default="c1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile-steps", type=int, default=200)
+    return ap.parse_args()
+
+
+def workload(name: str):
+    from sph2s_final_gb300 import scenes
+    if name == "c1":
+        sc = scenes.dam_break(1 / 256)
+        desc = "dam break 2,097,152 fluid + 2,043,880 boundary, s=1/256, h=2s, 128^3 cells, dt=2.5e-5"
+    else:
+        sc = scenes.dam_break(1 / 64)
+        desc = "dam break 32,768 fluid + 143,080 boundary, s=1/64, h=2s, 32^3 cells, dt=1e-4"
+    return sc, desc
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def physical_gpu_index(local: int) -> str:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        parts = [p.strip() for p in vis.split(",") if p.strip()]
+        if local < len(parts):
+            return parts[local]
+    return str(local)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: str):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", self.gpu], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, wl: str):
+    """Per-launch DRAM bytes of `kernel` on workload `wl` from the committed ncu summaries."""
+    pat = re.compile(rf"traffic_bytes_per_launch:\s*{re.escape(kernel)}\s+{wl}\s+([0-9.eE+]+)")
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = pat.search(f.read_text())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def boundary_touched(sc) -> int:
+    """Boundary particles within one cell (Chebyshev) of a fluid-occupied cell."""
+    from oracle import oracle as O  # host-side counting only
+    g = sc.config.grid
+    _, lf = O.cell_keys(g, sc.fluid.positions)
+    _, lb = O.cell_keys(g, sc.boundary.positions)
+    d = np.array(g.dims[:])
+    occ = np.zeros(d[::-1], bool)
+    cz, rem = np.divmod(lf, d[0] * d[1])
+    cy, cx = np.divmod(rem, d[0])
+    occ[cz, cy, cx] = True
+    dil = occ.copy()
+    for ax in range(3):
+        for sh in (-1, 1):
+            dil |= np.roll(occ, sh, axis=ax)  # roll wraps, but edges are clamped cells anyway
+    bz, rem = np.divmod(lb, d[0] * d[1])
+    by, bx = np.divmod(rem, d[0])
+    return int(dil[bz, by, bx].sum())
+
+
+def cpu_baseline(sc, seconds: float):
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    cores = O.num_threads()
+    ro = O.SSRollout(sc.config, sc.fluid.positions, sc.boundary.positions)
+    t0 = time.perf_counter()
+    ro.advance(sc.dt, 1)
+    t1 = time.perf_counter()
+    steps = max(1, int(seconds / max(t1 - t0, 1e-6)))
+    t2 = time.perf_counter()
+    ro.advance(sc.dt, steps)
+    t3 = time.perf_counter()
+    ro.close()
+    n = sc.fluid.num_particles
+    return {"value": n * steps / (t3 - t2), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"FP64 oracle (C++/OpenMP) on the same scene, {steps} steps after 1 warm-up step"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sc, desc = workload(args.workload)
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    cores = O.num_threads()
+    n = sc.fluid.num_particles
+    ro = O.SSRollout(sc.config, sc.fluid.positions, sc.boundary.positions)
+    t0 = time.perf_counter()
+    ro.advance(sc.dt, 1)
+    one = time.perf_counter() - t0
+    budget = 120.0
+    warm = min(args.warmup, max(0, int(0.2 * budget / one)))
+    steps = max(1, min(args.steps, int(budget / one)))
+    ro.advance(sc.dt, warm)
+    t0 = time.perf_counter()
+    ro.advance(sc.dt, steps)
+    el = time.perf_counter() - t0
+    ro.close()
+    v = n * steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
+        "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dam break)",
+        "config": {"workload": desc},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"FP64 CPU restatement of the reference step (the reference has "
+                                   f"no CPU path), {steps} of {args.steps} requested steps"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from sph2s_final_gb300.build import build_library
+    from sph2s_final_gb300.solver import Solver
+    from sph2s_final_gb300.solver import sort_passes_for
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build_library()
+    sc, desc = workload(args.workload)
+    n, nb = sc.fluid.num_particles, sc.boundary.num_particles
+    solver = Solver(sc.fluid, sc.boundary, sc.config)
+    stream = torch.cuda.ExternalStream(solver.stream)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    solver.advance(sc.dt, args.warmup)
+    solver.sync()
+    clocks = ClockSampler(physical_gpu_index(local))
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.advance(sc.dt, args.steps)
+    e1.record(stream)
+    solver.sync()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n * args.steps / (ms / 1e3)
+
+    # per-phase kernel durations (CUDA events on the solver's stream)
+    phases = solver.profile_phases(sc.dt, max(1, min(args.profile_steps, args.steps)))
+    solver.close()
+
+    # end to end through the public API: create from host arrays, then per step
+    # advance + positions read back into pinned host memory.
+    pinned = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    from sph2s_final_gb300 import _abi
+    barrier()
+    t0 = time.perf_counter()
+    s2 = Solver(sc.fluid, sc.boundary, sc.config)
+    for _ in range(args.steps):
+        s2.advance(sc.dt, 1)
+        _abi.check(_abi.lib().sph_get_positions(s2._h, _abi.fptr(pinned), _abi.SPH_ORDER_SORTED))
+    t1 = time.perf_counter()
+    s2.close()
+    e2e_s = t1 - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": ws * n * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(round((32 * n + 16 * nb) / args.steps)),
+           "d2h_bytes_per_step": 12 * n}
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = measured_peaks()
+    ncells = sc.config.grid.dims[0] * sc.config.grid.dims[1] * sc.config.grid.dims[2]
+    btouch = boundary_touched(sc)
+    force_bytes = 72 * n + 16 * ncells + 16 * btouch
+    dens_bytes = 28 * n + 8 * ncells
+    force_ms, dens_ms = phases["force"], phases["density"]
+    achieved = force_bytes / (force_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "force_kernel (force + integrate)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": committed_traffic("force_kernel", args.workload),
+                "algorithmic_bytes_per_launch": force_bytes,
+                "note": "FP32-issue bound: HBM fraction by compulsory bytes",
+                "density_kernel": {"ms": dens_ms, "achieved": dens_bytes / (dens_ms * 1e-3) / 1e9,
+                                   "algorithmic_bytes_per_launch": dens_bytes},
+                "phase_ms": phases}
+    passes = sort_passes_for(sc.config.grid)
+    launches = (5 + passes) * args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
+        "config": {"workload": desc, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "working set ~0.3 GB > 129 MB L2 (no flush needed)"},
+        "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

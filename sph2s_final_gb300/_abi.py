@@ -1,0 +1,112 @@
+"""ctypes binding of include/sph2s.h (libsph2s.so, built in-tree).
+
+There is no fallback: if the CUDA library is missing or fails to load, every
+call raises.  Build it with `python -m sph2s_final_gb300.build`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsph2s.so"
+
+SPH_OK = 0
+SPH_E_INVALID = 1
+SPH_E_CAPACITY = 2
+SPH_E_CUDA = 3
+SPH_E_TIMEOUT = 4
+SPH_ORDER_SORTED = 0
+SPH_ORDER_BY_ID = 1
+
+_STATUS = {1: "SPH_E_INVALID", 2: "SPH_E_CAPACITY", 3: "SPH_E_CUDA", 4: "SPH_E_TIMEOUT"}
+
+
+class SphError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class sph_grid(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("dims", C.c_int32 * 3), ("spacing", C.c_float)]
+
+
+class sph_config(C.Structure):
+    _fields_ = [
+        ("effective_radius", C.c_float),
+        ("fluid_particle_mass", C.c_float),
+        ("boundary_particle_mass", C.c_float),
+        ("rest_density", C.c_float),
+        ("bulk_modulus", C.c_float),
+        ("viscosity", C.c_float),
+        ("speed_sound", C.c_float),
+        ("tension_coefficient", C.c_float),
+        ("xsph_coeff", C.c_float),
+        ("grid", sph_grid),
+    ]
+
+
+_f = C.POINTER(C.c_float)
+_u = C.POINTER(C.c_uint32)
+_vp = C.c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "sph_make_grid": (C.c_int, [_f, _f, C.c_float, C.POINTER(sph_grid)]),
+    "sph_grid_num_cells": (C.c_uint32, [C.POINTER(sph_grid)]),
+    "sph_make_configuration": (C.c_int, [_f, _f, C.c_float, C.c_uint32, C.c_uint32, C.c_float,
+                                         C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.POINTER(sph_config)]),
+    "sph_particle_box": (C.c_int, [C.POINTER(sph_grid), _f, C.c_uint32, _u]),
+    "sph_particle_box_canvas": (C.c_int, [C.POINTER(sph_grid), C.c_int32, _f, C.c_uint32, _u]),
+    "sph_create": (C.c_int, [C.POINTER(sph_config), _f, C.c_uint32, _f, C.c_uint32, _f,
+                             C.POINTER(_vp)]),
+    "sph_advance": (C.c_int, [_vp, C.c_float, C.c_int32]),
+    "sph_sync": (C.c_int, [_vp]),
+    "sph_get_positions": (C.c_int, [_vp, _f, C.c_int32]),
+    "sph_get_velocities": (C.c_int, [_vp, _f, C.c_int32]),
+    "sph_get_densities": (C.c_int, [_vp, _f, C.c_int32]),
+    "sph_get_ids": (C.c_int, [_vp, _u]),
+    "sph_set_velocities": (C.c_int, [_vp, _f, C.c_int32]),
+    "sph_counts": (C.c_int, [_vp, _u, _u]),
+    "sph_stream": (C.c_void_p, [_vp]),
+    "sph_destroy": (C.c_int, [_vp]),
+    "sph_debug_step_fields": (C.c_int, [_vp, _u, _u, _u, _u, _u, _u, _f, _f]),
+    "sph_profile_phases": (C.c_int, [_vp, C.c_float, C.c_int32, _f]),
+    "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
+    "sph_last_error": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libsph2s.so once and declares every exported signature."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH.name} is not built; run `python -m sph2s_final_gb300.build` "
+                "(there is no CPU fallback)")
+        l = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != SPH_OK:
+        raise SphError(rc, lib().sph_last_error().decode(errors="replace"))
+
+
+def fptr(a):
+    return a.ctypes.data_as(_f) if a is not None else None
+
+
+def uptr(a):
+    return a.ctypes.data_as(_u) if a is not None else None

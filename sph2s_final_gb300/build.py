@@ -1,0 +1,121 @@
+"""In-tree build of libsph2s.so (nvcc, sm_103a only) and of the CPU oracle.
+
+The translation units are compiled in parallel and linked with nvcc; nothing is
+installed outside the repository.  `python -m sph2s_final_gb300.build` builds
+both libraries.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = ROOT / "_build"
+LIB = PKG / "libsph2s.so"
+ORACLE_SRC = ROOT / "oracle" / "sph_oracle.cpp"
+ORACLE_LIB = ROOT / "oracle" / "_build" / "liboracle.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3",
+    "-std=c++17",
+    "-lineinfo",
+    "--expt-relaxed-constexpr",
+    "-Xcompiler",
+    "-fPIC,-ffp-contract=off,-O2",
+] + ARCH
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found; the CUDA extension cannot be built")
+
+
+def _sources() -> list[Path]:
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
+
+
+def _headers() -> list[Path]:
+    return sorted(list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) +
+                  list((ROOT / "include").glob("*.h")))
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> Path:
+    srcs = _sources()
+    hdrs = _headers()
+    if not force and not _stale(LIB, srcs + hdrs + [Path(__file__)]):
+        return LIB
+    nvcc = _nvcc()
+    BUILD.mkdir(exist_ok=True)
+    objs = []
+    jobs = []
+    for s in srcs:
+        o = BUILD / (s.name + ".o")
+        objs.append(o)
+        cmd = [nvcc, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c", str(s), "-o", str(o)]
+        if ptxas_v and s.suffix == ".cu":
+            cmd[1:1] = ["-Xptxas", "-v"]
+        if force or _stale(o, [s] + hdrs + [Path(__file__)]):
+            jobs.append(cmd)
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return cmd, r
+
+    with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+        for cmd, r in ex.map(run, jobs):
+            if verbose or ptxas_v:
+                sys.stdout.write(r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    tmp = LIB.with_suffix(".so.tmp")
+    link = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcuda"]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Builds the CPU oracle (test infrastructure only)."""
+    if not force and not _stale(ORACLE_LIB, [ORACLE_SRC] + list(ORACLE_SRC.parent.glob("*.h"))):
+        return ORACLE_LIB
+    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    tmp = ORACLE_LIB.with_suffix(".so.tmp")
+    cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           str(ORACLE_SRC), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def main() -> None:
+    force = "--force" in sys.argv
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        a = ex.submit(build_library, force, "--verbose" in sys.argv, "--ptxas" in sys.argv)
+        b = ex.submit(build_oracle, force)
+        print(a.result())
+        print(b.result())
+
+
+if __name__ == "__main__":
+    main()

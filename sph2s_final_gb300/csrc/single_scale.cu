@@ -1,0 +1,440 @@
+// single_scale.cu -- the single-scale solver handle behind the C ABI.
+//
+// Replaces Solver (SPH2S_FINAL_SINGLE_SCALE/Solver.h:62-132, Solver.cu:898-1198):
+// the handle owns all device memory, keeps its configuration in kernel
+// parameters instead of one __constant__ symbol, runs on its own stream, and
+// captures one step into a CUDA graph that is replayed by sph_advance.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "errors.h"
+#include "host_params.h"
+#include "single_scale_kernels.cuh"
+
+using namespace sph;
+
+struct sph_solver {
+    sph_config cfg;
+    SimParams P;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0, nb = 0, ncells = 0;
+    int key_bits = 0;
+    float4* pos = nullptr;   // state, sorted order of the last step
+    float4* vel = nullptr;
+    float4* spos = nullptr;  // working copies in the current step's sorted order
+    float4* svel = nullptr;
+    float* rho = nullptr;
+    float2* aux = nullptr;
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* vals[2] = {nullptr, nullptr};
+    uint2* cells = nullptr;
+    uint2* bcells = nullptr;
+    float4* bpos = nullptr;
+    float* stage = nullptr;  // device staging for packed readback
+    void* sort_mem = nullptr;
+    SortScratch sort;
+    uint32_t* err = nullptr;  // device error word
+    uint32_t* err_host = nullptr;
+    int force_timeout = 0;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.0f;
+};
+
+namespace {
+
+int free_solver(sph_solver* s) {
+    if (!s) return SPH_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
+                    s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
+                    s->bpos,    s->sort_mem, s->err,     s->stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->err_host) cudaFreeHost(s->err_host);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return SPH_OK;
+}
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    SPH_CUDA(cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)));
+    return SPH_OK;
+}
+
+inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
+
+// hash -> onesweep sort -> reorder + cell ranges (Solver.cu:1098-1140).
+void enqueue_neighborhood(sph_solver* s) {
+    cudaStream_t st = s->stream;
+    int passes = sort_passes(s->key_bits);
+    cudaMemsetAsync(s->cells, 0xFF, sizeof(uint2) * s->ncells, st);
+    sort_reset(s->sort, st);
+    uint32_t hb = blocks_for(s->n);
+    if (hb > 152 * 8) hb = 152 * 8;
+    hash_hist_kernel<<<hb, 256, 0, st>>>(s->pos, s->n, s->P.g, passes, s->keys[0], s->sort.hist);
+    sort_scan(passes, s->sort, st);
+    int out = sort_passes_run(s->keys, s->vals, s->n, passes, s->sort, s->err, s->force_timeout, st);
+    gather_cells_kernel<true><<<blocks_for(s->n), 256, 0, st>>>(
+        s->keys[out], s->vals[out], s->n, s->P.g, s->pos, s->vel, s->spos, s->svel, s->cells,
+        s->err);
+}
+
+void enqueue_density(sph_solver* s) {
+    density_kernel<false><<<blocks_for(s->n), 256, 0, s->stream>>>(s->spos, s->cells, s->n, s->P,
+                                                                   s->rho, s->aux, nullptr);
+}
+
+void enqueue_force(sph_solver* s, float dt) {
+    force_kernel<0><<<blocks_for(s->n), 256, 0, s->stream>>>(
+        s->spos, s->svel, s->aux, s->cells, s->bpos, s->bcells, s->n, s->nb, s->P, dt, s->pos,
+        s->vel, nullptr, nullptr);
+}
+
+// One step: Solver::Advance (Solver.cu:1082-1096) with integrate fused into
+// the force pass.
+void enqueue_step(sph_solver* s, float dt) {
+    if (s->n == 0) return;
+    enqueue_neighborhood(s);
+    enqueue_density(s);
+    enqueue_force(s, dt);
+}
+
+int check_device_error(sph_solver* s) {
+    SPH_CUDA(cudaMemcpyAsync(s->err_host, s->err, 4, cudaMemcpyDeviceToHost, s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    uint32_t e = *s->err_host;
+    if (e) {
+        SPH_CUDA(cudaMemsetAsync(s->err, 0, 4, s->stream));
+        SPH_CUDA(cudaStreamSynchronize(s->stream));
+        if (e & kErrLookbackTimeout)
+            return fail(SPH_E_TIMEOUT, "radix sort look-back timed out; step results are invalid");
+        return fail(SPH_E_CAPACITY, "device-side capacity check failed");
+    }
+    return SPH_OK;
+}
+
+// Copies xyz of a float4 device array into a host AoS array, in sorted order
+// or by the persistent ids in pos.w; the packing runs on the device so the
+// host only receives 12 bytes per particle.
+int download_xyz(sph_solver* s, const float4* dsrc, float* dst, int32_t order) {
+    if (s->n == 0) return SPH_OK;
+    if (!s->stage) SPH_CUDA(cudaMalloc(&s->stage, 12 * (size_t)s->n));
+    pack_xyz_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(dsrc, s->pos, s->n,
+                                                             order == SPH_ORDER_BY_ID, s->stage);
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaMemcpyAsync(dst, s->stage, 12 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_fluid,
+               const float* boundary_xyz, uint32_t n_boundary, const float* velocity_xyz,
+               sph_solver** out) {
+    if (!config || !out) return fail(SPH_E_INVALID, "sph_create: NULL config or output handle");
+    *out = nullptr;
+    if (n_fluid && !fluid_xyz) return fail(SPH_E_INVALID, "sph_create: NULL fluid positions");
+    if (n_boundary && !boundary_xyz) return fail(SPH_E_INVALID, "sph_create: NULL boundary positions");
+    if (n_fluid > kMaxParticles || n_boundary > kMaxParticles)
+        return fail(SPH_E_CAPACITY, "sph_create: more than 2^30 particles");
+    SimParams P;
+    int rc = make_sim_params(*config, &P);
+    if (rc != SPH_OK) return rc;
+
+    sph_solver* s = new sph_solver();
+    s->cfg = *config;
+    s->P = P;
+    s->n = n_fluid;
+    s->nb = n_boundary;
+    s->ncells = sph_grid_num_cells(&config->grid);
+    s->key_bits = 3 * P.g.mbits;
+#define TRY(x)                      \
+    do {                            \
+        int _r = (x);               \
+        if (_r != SPH_OK) {         \
+            std::string m = sph_last_error(); \
+            free_solver(s);         \
+            return fail(_r, m);     \
+        }                           \
+    } while (0)
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    uint32_t nmax = n_fluid > n_boundary ? n_fluid : n_boundary;
+    TRY(dalloc(&s->pos, n_fluid));
+    TRY(dalloc(&s->vel, n_fluid));
+    TRY(dalloc(&s->spos, n_fluid));
+    TRY(dalloc(&s->svel, n_fluid));
+    TRY(dalloc(&s->rho, n_fluid));
+    TRY(dalloc(&s->aux, n_fluid));
+    TRY(dalloc(&s->keys[0], nmax));
+    TRY(dalloc(&s->keys[1], nmax));
+    TRY(dalloc(&s->vals[0], nmax));
+    TRY(dalloc(&s->vals[1], nmax));
+    TRY(dalloc(&s->cells, s->ncells));
+    TRY(dalloc(&s->bcells, s->ncells));
+    TRY(dalloc(&s->bpos, n_boundary));
+    TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
+    s->sort = sort_scratch_from(s->sort_mem, nmax);
+    TRY(dalloc(&s->err, 1));
+    TRY(check_cuda(cudaMallocHost((void**)&s->err_host, 4), "pinned", __FILE__, __LINE__));
+    TRY(check_cuda(cudaMemsetAsync(s->err, 0, 4, s->stream), "memset", __FILE__, __LINE__));
+    for (int b = 0; b < 2; ++b) {
+        TRY(check_cuda(cudaMemsetAsync(s->keys[b], 0, 4 * (size_t)(nmax ? nmax : 1), s->stream), "memset", __FILE__, __LINE__));
+        TRY(check_cuda(cudaMemsetAsync(s->vals[b], 0, 4 * (size_t)(nmax ? nmax : 1), s->stream), "memset", __FILE__, __LINE__));
+    }
+    TRY(check_cuda(cudaMemsetAsync(s->rho, 0, 4 * (size_t)(n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
+
+    // Upload the fluid state as float4 with the persistent id in w.
+    {
+        std::vector<float4> hp(n_fluid), hv(n_fluid);
+        for (uint32_t i = 0; i < n_fluid; ++i) {
+            float w;
+            std::memcpy(&w, &i, 4);
+            hp[i] = make_float4(fluid_xyz[3 * i], fluid_xyz[3 * i + 1], fluid_xyz[3 * i + 2], w);
+            hv[i] = velocity_xyz ? make_float4(velocity_xyz[3 * i], velocity_xyz[3 * i + 1],
+                                               velocity_xyz[3 * i + 2], 0.0f)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (n_fluid) {
+            TRY(check_cuda(cudaMemcpyAsync(s->pos, hp.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->vel, hv.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+        }
+        // Boundary: hashed and sorted once on the fluid grid (Solver.cu:1013-1055).
+        TRY(check_cuda(cudaMemsetAsync(s->bcells, 0xFF, sizeof(uint2) * s->ncells, s->stream), "memset", __FILE__, __LINE__));
+        if (n_boundary) {
+            std::vector<float4> hb(n_boundary);
+            for (uint32_t i = 0; i < n_boundary; ++i) {
+                float w;
+                std::memcpy(&w, &i, 4);
+                hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
+            }
+            float4* braw = nullptr;
+            TRY(dalloc(&braw, n_boundary));
+            cudaError_t e = cudaMemcpyAsync(braw, hb.data(), sizeof(float4) * n_boundary, cudaMemcpyHostToDevice, s->stream);
+            if (e == cudaSuccess) {
+                int passes = sort_passes(s->key_bits);
+                sort_reset(s->sort, s->stream);
+                hash_hist_kernel<<<blocks_for(n_boundary) > 1216 ? 1216 : blocks_for(n_boundary), 256, 0, s->stream>>>(
+                    braw, n_boundary, s->P.g, passes, s->keys[0], s->sort.hist);
+                sort_scan(passes, s->sort, s->stream);
+                int o = sort_passes_run(s->keys, s->vals, n_boundary, passes, s->sort, s->err, 0, s->stream);
+                gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
+                    s->keys[o], s->vals[o], n_boundary, s->P.g, braw, nullptr, s->bpos, nullptr, s->bcells,
+                    s->err);
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            }
+            cudaFree(braw);
+            TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
+        }
+        TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
+    }
+    TRY(check_device_error(s));
+#undef TRY
+    *out = s;
+    return SPH_OK;
+}
+
+int sph_advance(sph_solver* s, float dt, int32_t steps) {
+    if (!s) return fail(SPH_E_INVALID, "sph_advance: NULL handle");
+    if (steps < 0 || !std::isfinite(dt)) return fail(SPH_E_INVALID, "sph_advance: bad dt or steps");
+    if (s->n == 0 || steps == 0) return SPH_OK;
+    if (s->force_timeout) {
+        for (int k = 0; k < steps; ++k) enqueue_step(s, dt);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+    if (!s->graph || s->graph_dt != dt) {
+        if (s->graph) {
+            cudaGraphExecDestroy(s->graph);
+            s->graph = nullptr;
+        }
+        cudaGraph_t g;
+        SPH_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(s, dt);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        SPH_CUDA(le);
+        SPH_CUDA(ce);
+        cudaError_t ie = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        SPH_CUDA(ie);
+        s->graph_dt = dt;
+    }
+    for (int k = 0; k < steps; ++k) SPH_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    return SPH_OK;
+}
+
+int sph_sync(sph_solver* s) {
+    if (!s) return fail(SPH_E_INVALID, "sph_sync: NULL handle");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    return check_device_error(s);
+}
+
+int sph_get_positions(sph_solver* s, float* xyz, int32_t order) {
+    if (!s || (!xyz && s->n)) return fail(SPH_E_INVALID, "sph_get_positions: NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    return download_xyz(s, s->pos, xyz, order);
+}
+
+int sph_get_velocities(sph_solver* s, float* xyz, int32_t order) {
+    if (!s || (!xyz && s->n)) return fail(SPH_E_INVALID, "sph_get_velocities: NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    return download_xyz(s, s->vel, xyz, order);
+}
+
+int sph_get_densities(sph_solver* s, float* rho, int32_t order) {
+    if (!s || (!rho && s->n)) return fail(SPH_E_INVALID, "sph_get_densities: NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    std::vector<float> h(s->n);
+    std::vector<float4> p(s->n);
+    SPH_CUDA(cudaMemcpy(h.data(), s->rho, 4 * (size_t)s->n, cudaMemcpyDeviceToHost));
+    SPH_CUDA(cudaMemcpy(p.data(), s->pos, sizeof(float4) * s->n, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < s->n; ++k) {
+        uint32_t d = k;
+        if (order == SPH_ORDER_BY_ID) std::memcpy(&d, &p[k].w, 4);
+        if (d >= s->n) return fail(SPH_E_INVALID, "corrupt persistent id");
+        rho[d] = h[k];
+    }
+    return SPH_OK;
+}
+
+int sph_get_ids(sph_solver* s, uint32_t* ids) {
+    if (!s || (!ids && s->n)) return fail(SPH_E_INVALID, "sph_get_ids: NULL argument");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    std::vector<float4> p(s->n);
+    SPH_CUDA(cudaMemcpy(p.data(), s->pos, sizeof(float4) * s->n, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < s->n; ++k) std::memcpy(&ids[k], &p[k].w, 4);
+    return SPH_OK;
+}
+
+int sph_set_velocities(sph_solver* s, const float* xyz, int32_t order) {
+    if (!s || (!xyz && s->n)) return fail(SPH_E_INVALID, "sph_set_velocities: NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    std::vector<float4> p(s->n), v(s->n);
+    SPH_CUDA(cudaMemcpy(p.data(), s->pos, sizeof(float4) * s->n, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < s->n; ++k) {
+        uint32_t src = k;
+        if (order == SPH_ORDER_BY_ID) std::memcpy(&src, &p[k].w, 4);
+        if (src >= s->n) return fail(SPH_E_INVALID, "corrupt persistent id");
+        v[k] = make_float4(xyz[3 * src], xyz[3 * src + 1], xyz[3 * src + 2], 0.0f);
+    }
+    SPH_CUDA(cudaMemcpy(s->vel, v.data(), sizeof(float4) * s->n, cudaMemcpyHostToDevice));
+    return SPH_OK;
+}
+
+int sph_counts(sph_solver* s, uint32_t* n_fluid, uint32_t* n_boundary) {
+    if (!s) return fail(SPH_E_INVALID, "sph_counts: NULL handle");
+    if (n_fluid) *n_fluid = s->n;
+    if (n_boundary) *n_boundary = s->nb;
+    return SPH_OK;
+}
+
+void* sph_stream(sph_solver* s) { return s ? (void*)s->stream : nullptr; }
+
+int sph_destroy(sph_solver* s) { return free_solver(s); }
+
+int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t* cell_start,
+                          uint32_t* cell_end, uint32_t* nbr_fluid, uint32_t* nbr_boundary,
+                          float* rho, float* acc) {
+    if (!s) return fail(SPH_E_INVALID, "sph_debug_step_fields: NULL handle");
+    int rc = sph_sync(s);
+    if (rc != SPH_OK) return rc;
+    if (s->n == 0) return SPH_OK;
+    const uint32_t n = s->n;
+    float* drho = nullptr;
+    float2* daux = nullptr;
+    float* dacc = nullptr;
+    uint32_t *dnf = nullptr, *dnb = nullptr;
+    SPH_CUDA(cudaMalloc(&drho, 4 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&daux, 8 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&dacc, 12 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&dnf, 4 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&dnb, 4 * (size_t)n));
+    enqueue_neighborhood(s);
+    density_kernel<true><<<blocks_for(n), 256, 0, s->stream>>>(s->spos, s->cells, n, s->P, drho,
+                                                               daux, dnf);
+    force_kernel<1><<<blocks_for(n), 256, 0, s->stream>>>(s->spos, s->svel, daux, s->cells,
+                                                          s->bpos, s->bcells, n, s->nb, s->P, 0.0f,
+                                                          nullptr, nullptr, dacc, dnb);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    int out = sort_passes(s->key_bits) & 1;  // buffer index holding the sorted keys
+    std::vector<float4> sp;
+    if (e == cudaSuccess && keys) e = cudaMemcpy(keys, s->keys[out], 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && ids) {
+        sp.resize(n);
+        e = cudaMemcpy(sp.data(), s->spos, sizeof(float4) * n, cudaMemcpyDeviceToHost);
+        for (uint32_t k = 0; k < n && e == cudaSuccess; ++k) std::memcpy(&ids[k], &sp[k].w, 4);
+    }
+    if (e == cudaSuccess && (cell_start || cell_end)) {
+        std::vector<uint2> c(s->ncells);
+        e = cudaMemcpy(c.data(), s->cells, sizeof(uint2) * s->ncells, cudaMemcpyDeviceToHost);
+        for (uint32_t k = 0; k < s->ncells && e == cudaSuccess; ++k) {
+            if (cell_start) cell_start[k] = c[k].x;
+            if (cell_end) cell_end[k] = c[k].y;
+        }
+    }
+    if (e == cudaSuccess && nbr_fluid) e = cudaMemcpy(nbr_fluid, dnf, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nbr_boundary) e = cudaMemcpy(nbr_boundary, dnb, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && rho) e = cudaMemcpy(rho, drho, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && acc) e = cudaMemcpy(acc, dacc, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(drho);
+    cudaFree(daux);
+    cudaFree(dacc);
+    cudaFree(dnf);
+    cudaFree(dnb);
+    SPH_CUDA(e);
+    return check_device_error(s);
+}
+
+int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms) {
+    if (!s || !ms || steps < 0) return fail(SPH_E_INVALID, "sph_profile_phases: bad argument");
+    ms[0] = ms[1] = ms[2] = 0.0f;
+    if (s->n == 0 || steps == 0) return SPH_OK;
+    cudaEvent_t ev[4];
+    for (auto& e : ev) SPH_CUDA(cudaEventCreate(&e));
+    float acc[3] = {0, 0, 0};
+    cudaError_t err = cudaSuccess;
+    for (int k = 0; k < steps && err == cudaSuccess; ++k) {
+        cudaEventRecord(ev[0], s->stream);
+        enqueue_neighborhood(s);
+        cudaEventRecord(ev[1], s->stream);
+        enqueue_density(s);
+        cudaEventRecord(ev[2], s->stream);
+        enqueue_force(s, dt);
+        cudaEventRecord(ev[3], s->stream);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaEventSynchronize(ev[3]);
+        for (int p = 0; p < 3 && err == cudaSuccess; ++p) {
+            float t = 0.0f;
+            err = cudaEventElapsedTime(&t, ev[p], ev[p + 1]);
+            acc[p] += t;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    SPH_CUDA(err);
+    for (int p = 0; p < 3; ++p) ms[p] = acc[p] / (float)steps;
+    return check_device_error(s);
+}
+
+int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on) {
+    if (!s) return fail(SPH_E_INVALID, "NULL handle");
+    s->force_timeout = on ? 1 : 0;
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,72 @@
+"""Seeded synthetic dam-break scenes (the workloads the solver is measured on).
+
+A scene is a fluid lattice block in the unit box, jittered uniformly by
++-0.01 spacing per component, plus the hollow 5-layer boundary shell of the
+box built like ParticleData::CreateParticleBoxCanvas.  Constants follow the
+reference's single-scale driver (SPH2S_FINAL_SINGLE_SCALE/main.cpp:234-246:
+rest density 1000, K 30, mu 5, c 88.1472, sigma 0.8), with the support h = 2s
+and mass 1000 s^3 given directly instead of derived from a neighbour count.
+
+  dam_break(1/64)            32^3 = 32,768 particles, 32^3 cells, dt 1e-4
+  dam_break(1/256)           128^3 = 2,097,152 particles, 128^3 cells, dt 2.5e-5
+  dam_break(1/64, (32,64,32)) 65,536 particles (64 lattice sites along y)
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .solver import Grid, ParticleData, SolverConfiguration
+
+REST_DENSITY = 1000.0
+BULK_MODULUS = 30.0
+VISCOSITY = 5.0
+SPEED_SOUND = 88.1472
+TENSION = 0.8
+
+
+@dataclass
+class Scene:
+    fluid: ParticleData
+    boundary: ParticleData
+    config: object
+    dt: float
+    spacing: float
+
+
+def lattice_block(spacing: float, dims) -> np.ndarray:
+    """Lattice origin + (i, j, k) * s for i < dims (CreateParticleBox on dims)."""
+    g = Grid.make_grid_dims((0.0, 0.0, 0.0), dims, spacing)
+    return ParticleData.create_particle_box(g).positions
+
+
+def jitter(pos: np.ndarray, spacing: float, amount: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    j = rng.uniform(-amount * spacing, amount * spacing, size=pos.shape)
+    return (pos.astype(np.float64) + j).astype(np.float32)
+
+
+def dam_break(spacing: float, fluid_dims=None, seed: int = 0, jitter_amount: float = 0.01,
+              h_over_s: float = 2.0, border: int = 5, dt: float | None = None,
+              viscosity: float = VISCOSITY, bulk_modulus: float = BULK_MODULUS) -> Scene:
+    s = float(np.float32(spacing))
+    if fluid_dims is None:
+        k = int(round(0.5 / s))
+        fluid_dims = (k, k, k)
+    fluid = jitter(lattice_block(s, fluid_dims), s, jitter_amount, seed)
+    box = Grid.make_grid((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), s)
+    boundary = ParticleData.create_particle_box_canvas(box, border)
+    h = float(np.float32(h_over_s * s))
+    grid = Grid.make_grid((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), h)
+    mass = float(np.float32(REST_DENSITY * s ** 3))
+    cfg = SolverConfiguration.direct(h, mass, REST_DENSITY, bulk_modulus, viscosity, SPEED_SOUND,
+                                     TENSION, grid)
+    if dt is None:
+        dt = 1e-4 if s >= 1.0 / 64 else 2.5e-5
+    return Scene(ParticleData(fluid), boundary, cfg, dt, s)
+
+
+def small_scene(k: int = 8, seed: int = 0) -> Scene:
+    """A k^3 block at spacing 1/(2k) in the unit box (fast parity cases)."""
+    return dam_break(0.5 / k, (k, k, k), seed=seed, dt=1e-4)

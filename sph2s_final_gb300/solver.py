@@ -1,0 +1,236 @@
+"""Host-side mirror of the reference's Solver / ParticleData surface.
+
+Reference names, argument meaning and error behaviour are kept:
+
+  Grid.make_grid / Grid.compute_num_grid_cells    SPH2S_FINAL_SINGLE_SCALE/Grid.h:11-46
+  SolverConfiguration.make_configuration          SPH2S_FINAL_SINGLE_SCALE/Solver.h:15-48
+  ParticleData.create_particle_box(_canvas), union SPH2S_FINAL_SINGLE_SCALE/ParticleData.cpp:68-209
+  Solver(fluid, boundary, config).advance(dt)     SPH2S_FINAL_SINGLE_SCALE/Solver.h:113-121
+
+ParticleData is headless: positions live in a float32 (N, 3) array instead of
+an OpenGL VBO (the reference maps its VBOs into CUDA each step,
+ParticleData.cpp:47-66).  Every computation runs in libsph2s.so through the C
+ABI; errors raise SphError (the reference throws std::runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, fptr, lib, sph_config, sph_grid, uptr
+
+ORDER = {"sorted": _abi.SPH_ORDER_SORTED, "by_id": _abi.SPH_ORDER_BY_ID}
+
+
+class Grid:
+    """Grid::MakeGrid / ComputeNumGridCells / ComputeVolume."""
+
+    @staticmethod
+    def make_grid(origin, end, spacing: float) -> sph_grid:
+        g = sph_grid()
+        o = (C.c_float * 3)(*map(float, origin))
+        e = (C.c_float * 3)(*map(float, end))
+        check(lib().sph_make_grid(o, e, C.c_float(spacing), C.byref(g)))
+        return g
+
+    @staticmethod
+    def make_grid_dims(origin, dims, spacing: float) -> sph_grid:
+        """Grid::MakeGrid(origin, int3 dimensions, spacing), Grid.h:37-46."""
+        g = sph_grid()
+        g.origin[:] = [float(v) for v in origin]
+        g.dims[:] = [int(v) for v in dims]
+        g.spacing = float(np.float32(spacing))
+        return g
+
+    @staticmethod
+    def compute_num_grid_cells(g: sph_grid) -> int:
+        return int(lib().sph_grid_num_cells(C.byref(g)))
+
+    @staticmethod
+    def compute_volume(g: sph_grid) -> float:
+        """Grid::ComputeVolume (Grid.h:48-54), FP32 like the reference."""
+        s = np.float32(g.spacing)
+        n = np.float32(g.dims[0] * g.dims[1] * g.dims[2])
+        return float(np.float32(n * s * s * s))
+
+
+class SolverConfiguration:
+    @staticmethod
+    def make_configuration(origin, end, volume, num_particles, avg_particles, rest_density,
+                           bulk_modulus, viscosity, speed_sound, tension_coefficient,
+                           epsilon) -> sph_config:
+        c = sph_config()
+        o = (C.c_float * 3)(*map(float, origin))
+        e = (C.c_float * 3)(*map(float, end))
+        check(lib().sph_make_configuration(o, e, volume, num_particles, avg_particles,
+                                           rest_density, bulk_modulus, viscosity, speed_sound,
+                                           tension_coefficient, epsilon, C.byref(c)))
+        return c
+
+    @staticmethod
+    def direct(h, mass, rest_density, bulk_modulus, viscosity, speed_sound, tension_coefficient,
+               grid: sph_grid, boundary_mass=None, epsilon=0.0) -> sph_config:
+        """All constants explicit (h and m given directly rather than derived)."""
+        c = sph_config()
+        c.effective_radius = h
+        c.fluid_particle_mass = mass
+        c.boundary_particle_mass = mass if boundary_mass is None else boundary_mass
+        c.rest_density = rest_density
+        c.bulk_modulus = bulk_modulus
+        c.viscosity = viscosity
+        c.speed_sound = speed_sound
+        c.tension_coefficient = tension_coefficient
+        c.xsph_coeff = epsilon
+        c.grid = grid
+        return c
+
+
+@dataclass
+class ParticleData:
+    """Headless ParticleData: float32 positions (N, 3)."""
+
+    positions: np.ndarray
+
+    @property
+    def num_particles(self) -> int:
+        return int(self.positions.shape[0])
+
+    max_particles = num_particles
+
+    @staticmethod
+    def create_particle_box(g: sph_grid) -> "ParticleData":
+        n = C.c_uint32()
+        check(lib().sph_particle_box(C.byref(g), None, 0, C.byref(n)))
+        out = np.empty((n.value, 3), np.float32)
+        check(lib().sph_particle_box(C.byref(g), fptr(out), n.value, C.byref(n)))
+        return ParticleData(out)
+
+    @staticmethod
+    def create_particle_box_canvas(g: sph_grid, border: int) -> "ParticleData":
+        n = C.c_uint32()
+        check(lib().sph_particle_box_canvas(C.byref(g), border, None, 0, C.byref(n)))
+        out = np.empty((n.value, 3), np.float32)
+        check(lib().sph_particle_box_canvas(C.byref(g), border, fptr(out), n.value, C.byref(n)))
+        return ParticleData(out)
+
+    @staticmethod
+    def union(a: "ParticleData", b: "ParticleData") -> "ParticleData":
+        """ParticleData::Union (ParticleData.cpp:68-127): concatenation."""
+        if a is None or b is None:
+            return None
+        return ParticleData(np.concatenate([a.positions, b.positions]).astype(np.float32))
+
+
+def _as_xyz(a, n: int, what: str) -> np.ndarray:
+    arr = np.ascontiguousarray(a, dtype=np.float32).reshape(-1, 3)
+    if arr.shape[0] != n:
+        raise ValueError(f"{what}: expected {n} rows, got {arr.shape[0]}")
+    return arr
+
+
+class Solver:
+    """Single-scale WCSPH solver on the GPU (Solver, SPH2S_FINAL_SINGLE_SCALE/Solver.h:62-132)."""
+
+    def __init__(self, fluid: ParticleData, boundary: ParticleData | None, config: sph_config,
+                 velocities=None):
+        self.config = config
+        fx = np.ascontiguousarray(fluid.positions, np.float32)
+        bx = (np.ascontiguousarray(boundary.positions, np.float32) if boundary is not None
+              else np.zeros((0, 3), np.float32))
+        v = None if velocities is None else _as_xyz(velocities, fx.shape[0], "velocities")
+        h = C.c_void_p()
+        check(lib().sph_create(C.byref(config), fptr(fx), fx.shape[0], fptr(bx), bx.shape[0],
+                               fptr(v), C.byref(h)))
+        self._h = h
+        self.num_fluid = fx.shape[0]
+        self.num_boundary = bx.shape[0]
+
+    def bind(self) -> None:
+        """Solver::Bind: a no-op here; every handle carries its own configuration."""
+
+    def advance(self, dt: float, steps: int = 1) -> None:
+        check(lib().sph_advance(self._h, C.c_float(dt), int(steps)))
+
+    def sync(self) -> None:
+        check(lib().sph_sync(self._h))
+
+    def positions(self, order: str = "sorted") -> np.ndarray:
+        out = np.empty((self.num_fluid, 3), np.float32)
+        check(lib().sph_get_positions(self._h, fptr(out), ORDER[order]))
+        return out
+
+    def velocities(self, order: str = "sorted") -> np.ndarray:
+        out = np.empty((self.num_fluid, 3), np.float32)
+        check(lib().sph_get_velocities(self._h, fptr(out), ORDER[order]))
+        return out
+
+    def densities(self, order: str = "sorted") -> np.ndarray:
+        out = np.empty(self.num_fluid, np.float32)
+        check(lib().sph_get_densities(self._h, fptr(out), ORDER[order]))
+        return out
+
+    def ids(self) -> np.ndarray:
+        out = np.empty(self.num_fluid, np.uint32)
+        check(lib().sph_get_ids(self._h, uptr(out)))
+        return out
+
+    def set_velocities(self, v, order: str = "by_id") -> None:
+        a = _as_xyz(v, self.num_fluid, "velocities")
+        check(lib().sph_set_velocities(self._h, fptr(a), ORDER[order]))
+
+    @property
+    def stream(self) -> int:
+        return lib().sph_stream(self._h) or 0
+
+    def debug_step_fields(self) -> dict:
+        """Structure and fields of the next step for the current state (no advance)."""
+        n = self.num_fluid
+        nc = Grid.compute_num_grid_cells(self.config.grid)
+        r = {
+            "keys": np.empty(n, np.uint32), "ids": np.empty(n, np.uint32),
+            "cell_start": np.empty(nc, np.uint32), "cell_end": np.empty(nc, np.uint32),
+            "nbr_fluid": np.empty(n, np.uint32), "nbr_boundary": np.empty(n, np.uint32),
+            "rho": np.empty(n, np.float32), "acc": np.empty((n, 3), np.float32),
+        }
+        check(lib().sph_debug_step_fields(
+            self._h, uptr(r["keys"]), uptr(r["ids"]), uptr(r["cell_start"]), uptr(r["cell_end"]),
+            uptr(r["nbr_fluid"]), uptr(r["nbr_boundary"]), fptr(r["rho"]), fptr(r["acc"])))
+        return r
+
+    def profile_phases(self, dt: float, steps: int) -> dict:
+        """Mean ms per step of (neighbourhood, density, force+integrate), CUDA events."""
+        ms = np.zeros(3, np.float32)
+        check(lib().sph_profile_phases(self._h, C.c_float(dt), int(steps), fptr(ms)))
+        return {"neighborhood": float(ms[0]), "density": float(ms[1]), "force": float(ms[2])}
+
+    def debug_force_lookback_timeout(self, on: bool) -> None:
+        check(lib().sph_debug_force_lookback_timeout(self._h, 1 if on else 0))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def sort_passes_for(g: sph_grid) -> int:
+    """8-bit digit passes the onesweep sort runs for this grid's Morton keys."""
+    dmax = max(g.dims[0], g.dims[1], g.dims[2])
+    b = 1
+    while (1 << b) < dmax:
+        b += 1
+    return max(1, (3 * b + 7) // 8)
