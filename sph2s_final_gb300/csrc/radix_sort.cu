@@ -217,13 +217,14 @@ void sort_scan(int passes, const SortScratch& s, cudaStream_t st) {
     scan_kernel<<<1, 256, 0, st>>>(s.hist, passes);
 }
 
-int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int passes,
-                    const SortScratch& s, uint32_t* err, int force_timeout, cudaStream_t st) {
+int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals, uint32_t n,
+                    int passes, const SortScratch& s, uint32_t* err, int force_timeout,
+                    cudaStream_t st) {
     if (n == 0) return 0;
     uint32_t tiles = (n + kSortTile - 1) / kSortTile;
     int cur = 0;
     for (int p = 0; p < passes; ++p) {
-        const uint32_t* vin = (p == 0) ? vals[0] : vals[cur];
+        const uint32_t* vin = (p == 0) ? first_vals : vals[cur];
         onesweep_kernel<<<tiles, kSortThreads, 0, st>>>(
             keys[cur], vin, keys[cur ^ 1], vals[cur ^ 1], n, 8 * p, s.hist + p * 256,
             s.status + (size_t)p * s.max_tiles * 256, s.tile_ctr + p, err, force_timeout);
@@ -238,7 +239,7 @@ int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int key_bits,
     sort_reset(s, st);
     sort_histogram(keys[0], n, passes, s, st);
     sort_scan(passes, s, st);
-    return sort_passes_run(keys, vals, n, passes, s, err, force_timeout, st);
+    return sort_passes_run(keys, vals, vals[0], n, passes, s, err, force_timeout, st);
 }
 
 }  // namespace sph

@@ -57,13 +57,15 @@ void sort_histogram(const uint32_t* keys, uint32_t n, int passes, const SortScra
 // Turns the histograms into exclusive digit offsets (in place).
 void sort_scan(int passes, const SortScratch& s, cudaStream_t st);
 
-// Runs the digit passes.  keys[0]/vals[0] hold the input (vals[0] may be
-// NULL: values are then the input indices 0..n-1); keys[1]/vals[1] are the
-// alternate buffers.  Returns the index (0 or 1) of the buffers that hold the
-// sorted output.  `err` is a device word that receives SPH_E_TIMEOUT's bit on
-// a look-back timeout; `force_timeout` makes every look-back give up (test hook).
-int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int passes,
-                    const SortScratch& s, uint32_t* err, int force_timeout, cudaStream_t st);
+// Runs the digit passes.  keys[0] holds the input keys and first_vals the
+// input values (NULL: the values are the input indices 0..n-1, generated in
+// the first pass); keys[1]/vals[1] and vals[0] are ping-pong buffers.  Returns
+// the index (0 or 1) of the buffers that hold the sorted output.  `err` is a
+// device word that receives kErrLookbackTimeout on a look-back timeout;
+// `force_timeout` makes every look-back give up (test hook).
+int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals, uint32_t n,
+                    int passes, const SortScratch& s, uint32_t* err, int force_timeout,
+                    cudaStream_t st);
 
 // Convenience: reset + histogram + scan + passes.
 int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int key_bits,

@@ -75,7 +75,7 @@ void enqueue_neighborhood(sph_solver* s) {
     if (hb > 152 * 8) hb = 152 * 8;
     hash_hist_kernel<<<hb, 256, 0, st>>>(s->pos, s->n, s->P.g, passes, s->keys[0], s->sort.hist);
     sort_scan(passes, s->sort, st);
-    int out = sort_passes_run(s->keys, s->vals, s->n, passes, s->sort, s->err, s->force_timeout, st);
+    int out = sort_passes_run(s->keys, s->vals, nullptr, s->n, passes, s->sort, s->err, s->force_timeout, st);
     gather_cells_kernel<true><<<blocks_for(s->n), 256, 0, st>>>(
         s->keys[out], s->vals[out], s->n, s->P.g, s->pos, s->vel, s->spos, s->svel, s->cells,
         s->err);
@@ -221,7 +221,7 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
                 hash_hist_kernel<<<blocks_for(n_boundary) > 1216 ? 1216 : blocks_for(n_boundary), 256, 0, s->stream>>>(
                     braw, n_boundary, s->P.g, passes, s->keys[0], s->sort.hist);
                 sort_scan(passes, s->sort, s->stream);
-                int o = sort_passes_run(s->keys, s->vals, n_boundary, passes, s->sort, s->err, 0, s->stream);
+                int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort, s->err, 0, s->stream);
                 gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
                     s->keys[o], s->vals[o], n_boundary, s->P.g, braw, nullptr, s->bpos, nullptr, s->bcells,
                     s->err);
