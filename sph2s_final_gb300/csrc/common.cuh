@@ -12,6 +12,9 @@
 namespace sph {
 
 constexpr uint32_t kEmptyCell = 0xFFFFFFFFu;  // EMPTY_CELL_ID, SPH2S_FINAL_SINGLE_SCALE/Solver.cu:862
+// Neighbour-list slots per particle (about twice the ~34 neighbours at h = 2s);
+// particles with more neighbours fall back to a stencil rescan.
+constexpr int kMaxNbr = 64;
 
 struct GridParams {
     float ox, oy, oz;   // Grid::Origin

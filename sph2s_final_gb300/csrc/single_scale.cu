@@ -25,6 +25,9 @@ struct sph_solver {
     float4* svel = nullptr;
     float* rho = nullptr;
     float2* aux = nullptr;
+    uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
+    uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
+    uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
     uint2* cells = nullptr;
@@ -48,7 +51,8 @@ int free_solver(sph_solver* s) {
     if (s->graph) cudaGraphExecDestroy(s->graph);
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
-                    s->bpos,    s->sort_mem, s->err,     s->stage};
+                    s->bpos,    s->sort_mem, s->err,     s->stage, s->nbr, s->nbr_count,
+                    s->bnear};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->err_host) cudaFreeHost(s->err_host);
@@ -82,14 +86,14 @@ void enqueue_neighborhood(sph_solver* s) {
 }
 
 void enqueue_density(sph_solver* s) {
-    density_kernel<false><<<blocks_for(s->n), 256, 0, s->stream>>>(s->spos, s->cells, s->n, s->P,
-                                                                   s->rho, s->aux, nullptr);
+    density_kernel<false><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
+        s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, nullptr);
 }
 
 void enqueue_force(sph_solver* s, float dt) {
     force_kernel<0><<<blocks_for(s->n), 256, 0, s->stream>>>(
-        s->spos, s->svel, s->aux, s->cells, s->bpos, s->bcells, s->n, s->nb, s->P, dt, s->pos,
-        s->vel, nullptr, nullptr);
+        s->spos, s->svel, s->aux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
+        s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr);
 }
 
 // One step: Solver::Advance (Solver.cu:1082-1096) with integrate fused into
@@ -170,6 +174,9 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     TRY(dalloc(&s->svel, n_fluid));
     TRY(dalloc(&s->rho, n_fluid));
     TRY(dalloc(&s->aux, n_fluid));
+    TRY(dalloc(&s->nbr, (size_t)n_fluid * (kMaxNbr / 4)));
+    TRY(dalloc(&s->nbr_count, n_fluid));
+    TRY(dalloc(&s->bnear, s->ncells));
     TRY(dalloc(&s->keys[0], nmax));
     TRY(dalloc(&s->keys[1], nmax));
     TRY(dalloc(&s->vals[0], nmax));
@@ -231,6 +238,10 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
             cudaFree(braw);
             TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
         }
+        const int reach = (int)std::ceil(config->effective_radius / config->grid.spacing) + 1;
+        boundary_near_kernel<<<blocks_for(s->ncells), 256, 0, s->stream>>>(s->bcells, s->P.g, reach,
+                                                                           s->bnear);
+        TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
         TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
     }
     TRY(check_device_error(s));
@@ -365,11 +376,11 @@ int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t
     SPH_CUDA(cudaMalloc(&dnf, 4 * (size_t)n));
     SPH_CUDA(cudaMalloc(&dnb, 4 * (size_t)n));
     enqueue_neighborhood(s);
-    density_kernel<true><<<blocks_for(n), 256, 0, s->stream>>>(s->spos, s->cells, n, s->P, drho,
-                                                               daux, dnf);
-    force_kernel<1><<<blocks_for(n), 256, 0, s->stream>>>(s->spos, s->svel, daux, s->cells,
-                                                          s->bpos, s->bcells, n, s->nb, s->P, 0.0f,
-                                                          nullptr, nullptr, dacc, dnb);
+    density_kernel<true><<<blocks_for(n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
+        s->spos, s->cells, n, s->P, drho, daux, s->nbr, s->nbr_count, dnf);
+    force_kernel<1><<<blocks_for(n), 256, 0, s->stream>>>(
+        s->spos, s->svel, daux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear, n,
+        s->nb, s->P, 0.0f, nullptr, nullptr, dacc, dnb);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     int out = sort_passes(s->key_bits) & 1;  // buffer index holding the sorted keys
