@@ -1,0 +1,133 @@
+// force_kernel.cuh -- the force + integrate pass of the single-scale step.
+//
+// computeAccelerationsD + integrateD (SPH2S_FINAL_SINGLE_SCALE/Solver.cu:601-755,
+// with the pair terms of computeAccelerationCell / computeBoundaryForceCell,
+// Solver.cu:231-344).  Fluid neighbours come from the density pass's list.
+#pragma once
+#include "common.cuh"
+
+namespace sph {
+
+// Pair term of the force pass for one fluid neighbour j (0 < r2 < T).
+struct ForceAcc {
+    float fx, fy, fz;  // sum of s_ij * x_ij
+    float wx, wy, wz;  // sum of (h - r) / rho_j * (v_j - v_i)
+};
+
+__device__ __forceinline__ void force_pair(ForceAcc& A, const SimParams& P, float ai_x, float tcoef,
+                                           const float4& vi, float dx, float dy, float dz,
+                                           float r2, const float2& aj, const float4& vj) {
+    float rs = rsqrtf(r2);
+    float hr = P.h - r2 * rs;
+    float a = P.h2 - r2;
+    float sc = P.pres_coef * (ai_x + aj.x) * hr * hr * rs - tcoef * a * a * a;
+    A.fx = fmaf(sc, dx, A.fx);
+    A.fy = fmaf(sc, dy, A.fy);
+    A.fz = fmaf(sc, dz, A.fz);
+    float vc = aj.y * hr;
+    A.wx = fmaf(vc, vj.x - vi.x, A.wx);
+    A.wy = fmaf(vc, vj.y - vi.y, A.wy);
+    A.wz = fmaf(vc, vj.z - vi.z, A.wz);
+}
+
+// Pressure (spiky gradient), viscosity (Laplacian), tension (Poly6), boundary
+// force and gravity; MODE 0 integrates (symplectic Euler) into pos_out/vel_out,
+// MODE 1 writes the acceleration and the boundary neighbour count instead.
+template <int MODE>
+__global__ void __launch_bounds__(256) force_kernel(
+    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ aux,
+    const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
+    const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
+    const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
+    SimParams P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = pos[i];
+    const float4 vi = vel[i];
+    const float2 ai = aux[i];
+    const float tcoef = P.tens_coef * ai.y;
+    ForceAcc A = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const uint32_t kc = nbr_count[i];
+    if (kc <= (uint32_t)kMaxNbr) {
+        for (uint32_t t = 0; t < kc; t += 4) {
+            const uint4 g = __ldg(&nbr4[(size_t)(t >> 2) * n + i]);
+            const uint32_t js[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (t + u < kc) {
+                    const uint32_t j = min(js[u], n - 1);
+                    const float4 xj = __ldg(&pos[j]);
+                    float dx, dy, dz;
+                    float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+                    force_pair(A, P, ai.x, tcoef, vi, dx, dy, dz, r2, __ldg(&aux[j]),
+                               __ldg(&vel[j]));
+                }
+            }
+        }
+    } else {
+        const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+        for (int cz = s.z0; cz <= s.z1; ++cz)
+            for (int cy = s.y0; cy <= s.y1; ++cy) {
+                const uint32_t row = linear_cell(P.g, 0, cy, cz);
+                for (int cx = s.x0; cx <= s.x1; ++cx) {
+                    const uint2 r = __ldg(&cells[row + cx]);
+                    const uint32_t e = min(r.y, n);
+                    for (uint32_t j = r.x; j < e; ++j) {
+                        const float4 xj = __ldg(&pos[j]);
+                        float dx, dy, dz;
+                        float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+                        if (r2 < P.T && r2 != 0.0f)
+                            force_pair(A, P, ai.x, tcoef, vi, dx, dy, dz, r2, __ldg(&aux[j]),
+                                       __ldg(&vel[j]));
+                    }
+                }
+            }
+    }
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    uint32_t bcnt = 0;
+    const uint32_t home = linear_cell(P.g, cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx),
+                                      cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy),
+                                      cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz));
+    if (__ldg(&bnear[home])) {
+        const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+        for (int cz = s.z0; cz <= s.z1; ++cz)
+            for (int cy = s.y0; cy <= s.y1; ++cy) {
+                const uint32_t row = linear_cell(P.g, 0, cy, cz);
+                for (int cx = s.x0; cx <= s.x1; ++cx) {
+                    const uint2 r = __ldg(&bcells[row + cx]);
+                    const uint32_t e = min(r.y, nb);
+                    for (uint32_t j = r.x; j < e; ++j) {
+                        const float4 xj = __ldg(&bpos[j]);
+                        float dx, dy, dz;
+                        float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+                        if (r2 < P.T) {
+                            float rs = rsqrtf(r2);
+                            float q = r2 * rs * P.two_over_h;
+                            float w = P.bnd_coef * boundary_shape(q) * rs * rs;
+                            bx = fmaf(w, dx, bx);
+                            by = fmaf(w, dy, by);
+                            bz = fmaf(w, dz, bz);
+                            if (MODE == 1) ++bcnt;
+                        }
+                    }
+                }
+            }
+    }
+    const float vf = P.visc_coef * ai.y;
+    const float axx = fmaf(vf, A.wx, A.fx) + bx;
+    const float ayy = fmaf(vf, A.wy, A.fy) + P.gravity + by;
+    const float azz = fmaf(vf, A.wz, A.fz) + bz;
+    if (MODE == 0) {
+        float nvx = fmaf(dt, axx, vi.x), nvy = fmaf(dt, ayy, vi.y), nvz = fmaf(dt, azz, vi.z);
+        pos_out[i] = make_float4(fmaf(dt, nvx, xi.x), fmaf(dt, nvy, xi.y), fmaf(dt, nvz, xi.z), xi.w);
+        vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
+    } else {
+        acc_out[3 * i + 0] = axx;
+        acc_out[3 * i + 1] = ayy;
+        acc_out[3 * i + 2] = azz;
+        nbr_b[i] = bcnt;
+    }
+}
+
+}  // namespace sph
