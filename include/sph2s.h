@@ -141,6 +141,19 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms);
  * bounded spin, so the next sph_sync returns SPH_E_TIMEOUT without hanging. */
 int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on);
 
+/* ---- key-value sort ------------------------------------------------------ */
+
+/* Stable ascending sort of n (uint32 key, uint32 value) pairs in device
+ * memory by the low `key_bits` bits of the key (the higher bits must be 0):
+ * the hand-written onesweep radix sort the step uses, replacing
+ * thrust::sort_by_key (SPH2S_FINAL_SINGLE_SCALE/Solver.cu:1110-1115).
+ * vals_in may be NULL (values are then 0..n-1).  Inputs are not modified; the
+ * outputs must not overlap them.  Enqueues on `stream` (a cudaStream_t, NULL
+ * = legacy default stream), allocates its scratch with cudaMalloc, and
+ * returns after the sort completed. */
+int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                   uint32_t* vals_out, uint32_t n, int32_t key_bits, void* stream);
+
 /* Description of the last failure on the calling thread ("" if none). */
 const char* sph_last_error(void);
 

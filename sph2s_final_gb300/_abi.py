@@ -76,6 +76,8 @@ SIGNATURES = {
     "sph_debug_step_fields": (C.c_int, [_vp, _u, _u, _u, _u, _u, _u, _f, _f]),
     "sph_profile_phases": (C.c_int, [_vp, C.c_float, C.c_int32, _f]),
     "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
+    "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                 C.c_int32, C.c_void_p]),
     "sph_last_error": (C.c_char_p, []),
 }
 

@@ -217,6 +217,16 @@ void sort_scan(int passes, const SortScratch& s, cudaStream_t st) {
     scan_kernel<<<1, 256, 0, st>>>(s.hist, passes);
 }
 
+void sort_pass(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+               uint32_t* vals_out, uint32_t n, int p, const SortScratch& s, uint32_t* err,
+               int force_timeout, cudaStream_t st) {
+    if (n == 0) return;
+    uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+    onesweep_kernel<<<tiles, kSortThreads, 0, st>>>(
+        keys_in, vals_in, keys_out, vals_out, n, 8 * p, s.hist + p * 256,
+        s.status + (size_t)p * s.max_tiles * 256, s.tile_ctr + p, err, force_timeout);
+}
+
 int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals, uint32_t n,
                     int passes, const SortScratch& s, uint32_t* err, int force_timeout,
                     cudaStream_t st) {

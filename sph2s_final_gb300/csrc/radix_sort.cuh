@@ -67,6 +67,13 @@ int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_
                     int passes, const SortScratch& s, uint32_t* err, int force_timeout,
                     cudaStream_t st);
 
+// One digit pass p (bits 8p..8p+7) from explicit input to output buffers
+// (vals_in NULL: values are the input indices).  Needs the histograms of
+// sort_histogram + sort_scan in `s`.
+void sort_pass(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+               uint32_t* vals_out, uint32_t n, int p, const SortScratch& s, uint32_t* err,
+               int force_timeout, cudaStream_t st);
+
 // Convenience: reset + histogram + scan + passes.
 int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int key_bits,
                const SortScratch& s, uint32_t* err, int force_timeout, cudaStream_t st);
