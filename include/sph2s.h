@@ -154,6 +154,20 @@ int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on);
 int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                    uint32_t* vals_out, uint32_t n, int32_t key_bits, void* stream);
 
+/* sph_sort_pairs for callers that cannot allocate device memory (no
+ * counterpart in the reference): hosts that own a fixed device-memory budget
+ * and pass only their own buffers, code running while a global-mode stream
+ * capture is open elsewhere (cudaMalloc is illegal then), or loops that must
+ * not risk an allocation's implicit synchronisation.  Same arguments and
+ * results as sph_sort_pairs; calls no cudaMalloc/cudaFree.  Its scratch is one
+ * static device array of about 10 MB that each GPU loading the library holds
+ * until exit, which limits n to 1,048,576 pairs (larger n: SPH_E_CAPACITY).
+ * The first call on a device looks the array up (make it before any stream
+ * capture); all calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                           uint32_t* vals_out, uint32_t n, int32_t key_bits, void* stream);
+
 /* Description of the last failure on the calling thread ("" if none). */
 const char* sph_last_error(void);
 

@@ -78,6 +78,8 @@ SIGNATURES = {
     "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
     "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                  C.c_int32, C.c_void_p]),
+    "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_uint32, C.c_int32, C.c_void_p]),
     "sph_last_error": (C.c_char_p, []),
 }
 
