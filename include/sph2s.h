@@ -141,6 +141,77 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms);
  * bounded spin, so the next sph_sync returns SPH_E_TIMEOUT without hanging. */
 int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on);
 
+/* ---- two-scale solver -------------------------------------------------- */
+
+#define SPH_LOW 0  /* coarse population: support h, mass m */
+#define SPH_HIGH 1 /* fine population: support h/2, mass m/8 */
+
+/* SolverConfiguration of the two-scale project (SPH2S_FINAL_TWO_SCALE/Solver.h:52-61)
+ * plus the refinement slab that drives splitting and merging (not in the
+ * reference, whose split trigger is commented out, Solver.cu:1077-1082):
+ * a LOW particle in state 0 strictly inside refine_lo < x[refine_axis] <
+ * refine_hi at the start of a step splits into 8 HIGH children; a group of
+ * 8 children, all fully blended in, whose centroid is outside the slab
+ * merges back into one LOW particle.  refine_axis = -1 disables both. */
+typedef struct sph_config2 {
+    float effective_radius[2];    /* [SPH_LOW] h, [SPH_HIGH] h/2 */
+    float fluid_particle_mass[2]; /* m, m/8 */
+    float boundary_particle_mass; /* used with the LOW radius for both populations */
+    float rest_density;
+    float bulk_modulus;
+    float viscosity;
+    float speed_sound;
+    float tension_coefficient;
+    float blend_increment;        /* lambda change per step (BlendIncrement) */
+    sph_grid grid[2];             /* one grid per population, spacing = its support */
+    int32_t refine_axis;          /* 0, 1, 2 or -1 */
+    float refine_lo, refine_hi;
+} sph_config2;
+
+typedef struct sph_solver2 sph_solver2;
+
+/* SolverConfiguration::MakeConfiguration of the two-scale project
+ * (SPH2S_FINAL_TWO_SCALE/Solver.h:16-50); refinement disabled. */
+int sph_make_configuration2(const float origin[3], const float end[3], float volume,
+                            uint32_t num_particles, uint32_t avg_particles, float rest_density,
+                            float bulk_modulus, float viscosity, float speed_sound,
+                            float tension_coefficient, float blend_increment, sph_config2* out);
+
+/* Solver(low, high, boundary, config) + Bind() (SPH2S_FINAL_TWO_SCALE/Solver.h:121-130,
+ * Solver.cu:1444-1544): LOW particles start in state 0, HIGH in state 4, all
+ * with lambda 1 and zero velocity; the boundary is sorted once on the LOW
+ * grid.  Capacities bound the populations (0 = 2 n_low + 1024 and
+ * 8 (n_low + n_high) + 1024; the reference allocates 8 x LOW for HIGH). */
+int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
+                const float* high_xyz, uint32_t n_high, const float* boundary_xyz,
+                uint32_t n_boundary, uint32_t capacity_low, uint32_t capacity_high,
+                sph_solver2** out);
+/* Solver::Advance (SPH2S_FINAL_TWO_SCALE/Solver.cu:1568-1614), `steps` times;
+ * synchronous (the population sizes are read back after every step, like
+ * the reference's per-step count read, Solver.cu:1633-1638). */
+int sph2_advance(sph_solver2* s, float dt, int32_t steps);
+int sph2_counts(sph_solver2* s, uint32_t* n_low, uint32_t* n_high, uint32_t* n_boundary,
+                uint32_t* groups);
+/* Persistent id the next particle created in each population will get
+ * (children and merged particles receive consecutive ids). */
+int sph2_next_ids(sph_solver2* s, uint32_t* next_low, uint32_t* next_high);
+/* Counters of the last step: splits, merges, removed LOW, removed HIGH,
+ * fade-in completions LOW, HIGH. */
+int sph2_last_stats(sph_solver2* s, uint32_t* stats6);
+/* State of one population in its current order (each pointer optional):
+ * positions, velocities (3 floats each), blend coefficients, state bits,
+ * group ids (0xFFFFFFFF = none) and persistent ids. */
+int sph2_get_state(sph_solver2* s, int32_t population, float* xyz, float* vel, float* lambda,
+                   int32_t* state, uint32_t* group, uint32_t* ids);
+/* Parity instrumentation: for the current state, without advancing, the
+ * sorted persistent ids, densities, accelerations and neighbour counts (same
+ * population, complementary population, boundary) of one population, in the
+ * sorted order of the next step. */
+int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sorted, float* rho,
+                           float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
+                           uint32_t* nbr_boundary);
+int sph2_destroy(sph_solver2* s);
+
 /* ---- key-value sort ------------------------------------------------------ */
 
 /* Stable ascending sort of n (uint32 key, uint32 value) pairs in device

@@ -48,6 +48,24 @@ class sph_config(C.Structure):
     ]
 
 
+class sph_config2(C.Structure):
+    _fields_ = [
+        ("effective_radius", C.c_float * 2),
+        ("fluid_particle_mass", C.c_float * 2),
+        ("boundary_particle_mass", C.c_float),
+        ("rest_density", C.c_float),
+        ("bulk_modulus", C.c_float),
+        ("viscosity", C.c_float),
+        ("speed_sound", C.c_float),
+        ("tension_coefficient", C.c_float),
+        ("blend_increment", C.c_float),
+        ("grid", sph_grid * 2),
+        ("refine_axis", C.c_int32),
+        ("refine_lo", C.c_float),
+        ("refine_hi", C.c_float),
+    ]
+
+
 _f = C.POINTER(C.c_float)
 _u = C.POINTER(C.c_uint32)
 _vp = C.c_void_p
@@ -76,6 +94,18 @@ SIGNATURES = {
     "sph_debug_step_fields": (C.c_int, [_vp, _u, _u, _u, _u, _u, _u, _f, _f]),
     "sph_profile_phases": (C.c_int, [_vp, C.c_float, C.c_int32, _f]),
     "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
+    "sph_make_configuration2": (C.c_int, [_f, _f, C.c_float, C.c_uint32, C.c_uint32, C.c_float,
+                                          C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                          C.POINTER(sph_config2)]),
+    "sph2_create": (C.c_int, [C.POINTER(sph_config2), _f, C.c_uint32, _f, C.c_uint32, _f,
+                              C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(_vp)]),
+    "sph2_advance": (C.c_int, [_vp, C.c_float, C.c_int32]),
+    "sph2_counts": (C.c_int, [_vp, _u, _u, _u, _u]),
+    "sph2_last_stats": (C.c_int, [_vp, _u]),
+    "sph2_next_ids": (C.c_int, [_vp, _u, _u]),
+    "sph2_get_state": (C.c_int, [_vp, C.c_int32, _f, _f, _f, C.POINTER(C.c_int32), _u, _u]),
+    "sph2_debug_step_fields": (C.c_int, [_vp, C.c_int32, _u, _f, _f, _u, _u, _u]),
+    "sph2_destroy": (C.c_int, [_vp]),
     "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libsph2s.so"
-ORACLE_SRC = ROOT / "oracle" / "sph_oracle.cpp"
+ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ROOT / "oracle" / "_build" / "liboracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -94,13 +94,14 @@ def build_library(force: bool = False, verbose: bool = False, ptxas_v: bool = Fa
 
 def build_oracle(force: bool = False) -> Path:
     """Builds the CPU oracle (test infrastructure only)."""
-    if not force and not _stale(ORACLE_LIB, [ORACLE_SRC] + list(ORACLE_SRC.parent.glob("*.h"))):
+    srcs = sorted(ORACLE_DIR.glob("*.cpp"))
+    if not force and not _stale(ORACLE_LIB, srcs + list(ORACLE_DIR.glob("*.h"))):
         return ORACLE_LIB
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     cxx = os.environ.get("CXX", "g++")
     tmp = ORACLE_LIB.with_suffix(".so.tmp")
     cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           str(ORACLE_SRC), "-o", str(tmp)]
+           *map(str, srcs), "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

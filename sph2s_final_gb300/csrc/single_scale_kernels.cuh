@@ -17,7 +17,7 @@
 namespace sph {
 
 // Morton key per particle, fused with the digit histograms of every sort pass.
-__global__ void __launch_bounds__(256) hash_hist_kernel(const float4* __restrict__ pos, uint32_t n,
+static __global__ void __launch_bounds__(256) hash_hist_kernel(const float4* __restrict__ pos, uint32_t n,
                                                         GridParams g, int passes,
                                                         uint32_t* __restrict__ keys,
                                                         uint32_t* __restrict__ hist) {
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
 
 // Packs xyz of a float4 array into AoS floats, in sorted order or scattered
 // to the persistent ids held in ids[k].w.
-__global__ void __launch_bounds__(256) pack_xyz_kernel(const float4* __restrict__ src,
+static __global__ void __launch_bounds__(256) pack_xyz_kernel(const float4* __restrict__ src,
                                                        const float4* __restrict__ ids, uint32_t n,
                                                        int by_id, float* __restrict__ dst) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) pack_xyz_kernel(const float4* __restrict_
 // cell?  A particle's stencil [cell(x-h), cell(x+h)] never leaves
 // cell(x) +- (ceil(h/spacing) + 1), so particles in cells without the flag
 // skip the boundary stencil without changing any result.
-__global__ void __launch_bounds__(256) boundary_near_kernel(const uint2* __restrict__ bcells,
+static __global__ void __launch_bounds__(256) boundary_near_kernel(const uint2* __restrict__ bcells,
                                                             GridParams g, int reach,
                                                             uint8_t* __restrict__ near) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;

@@ -1,0 +1,576 @@
+// two_scale.cu -- the two-scale solver handle behind the C ABI.
+//
+// Replaces the two-scale Solver (SPH2S_FINAL_TWO_SCALE/Solver.h:64-144,
+// Solver.cu:1333-1771).  Step order follows Solver::Advance (Solver.cu:1568-1614):
+// neighbourhoods of both populations, densities, accelerations, integration;
+// split children and merged particles are placed by prefix-sum compaction
+// instead of the reference's atomicAdd re-listing, so every step is
+// deterministic.  The host reads the new population sizes back after each
+// step, as the reference does (Solver.cu:1633-1638).
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "errors.h"
+#include "host_params.h"
+#include "radix_sort.cuh"
+#include "scan.cuh"
+#include "single_scale_kernels.cuh"
+#include "two_scale_kernels.cuh"
+
+using namespace sph;
+
+namespace {
+
+struct Pop {
+    uint32_t n = 0, cap = 0, ncells = 0;
+    int key_bits = 0;
+    float4 *pos = nullptr, *vel = nullptr;
+    int32_t* stt = nullptr;
+    uint32_t* grp = nullptr;
+    float4 *spos = nullptr, *svel = nullptr;
+    int32_t* sstt = nullptr;
+    uint32_t* sgrp = nullptr;
+    float* rho = nullptr;
+    float2* aux = nullptr;
+    float4 *ipos = nullptr, *ivel = nullptr;
+    int32_t* istt = nullptr;
+    uint32_t *igrp = nullptr, *keep = nullptr, *off = nullptr, *split = nullptr, *soff = nullptr;
+    uint2* cells = nullptr;
+};
+
+template <class T>
+int dalloc(T** p, size_t count, std::vector<void*>& owned) {
+    SPH_CUDA(cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)));
+    owned.push_back(*p);
+    return SPH_OK;
+}
+
+inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
+
+}  // namespace
+
+struct sph_solver2 {
+    sph_config2 cfg;
+    TSParams P;
+    cudaStream_t stream = nullptr;
+    Pop pop[2];
+    uint32_t nb = 0;
+    float4* bpos = nullptr;
+    uint2* bcells = nullptr;
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* vals[2] = {nullptr, nullptr};
+    void* sort_mem = nullptr;
+    SortScratch sort;
+    uint32_t* scan_scratch = nullptr;
+    uint32_t* tot = nullptr;
+    uint32_t cap_groups = 0;
+    unsigned long long* gsum = nullptr;
+    uint32_t* gready = nullptr;
+    uint32_t* gmerge = nullptr;
+    uint32_t* moff = nullptr;
+    unsigned long long* gacc = nullptr;
+    uint32_t* ctl = nullptr;
+    uint32_t* ctl_host = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t group_base = 0;
+    uint32_t stats[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t next_id[2] = {0, 0};  // persistent id of the next particle created (LOW, HIGH)
+    std::vector<void*> owned;
+};
+
+namespace {
+
+int free_solver2(sph_solver2* s) {
+    if (!s) return SPH_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->owned) cudaFree(p);
+    if (s->ctl_host) cudaFreeHost(s->ctl_host);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return SPH_OK;
+}
+
+int make_ts_params(const sph_config2& c, TSParams* out) {
+    for (int r = 0; r < 2; ++r) {
+        int rc = validate_grid(c.grid[r], "sph_config2");
+        if (rc != SPH_OK) return rc;
+        if (!(c.effective_radius[r] > 0.0f) || !(c.fluid_particle_mass[r] > 0.0f))
+            return fail(SPH_E_INVALID, "sph_config2: radii and masses must be positive");
+    }
+    if (c.refine_axis > 2) return fail(SPH_E_INVALID, "sph_config2: refine_axis must be -1..2");
+    const double pi = 3.14159265358979323846;
+    TSParams P;
+    for (int r = 0; r < 2; ++r) {
+        const double h = c.effective_radius[r], h3 = h * h * h;
+        P.g[r] = make_grid_params(c.grid[r]);
+        P.h[r] = c.effective_radius[r];
+        P.h2[r] = P.h[r] * P.h[r];
+        P.T[r] = neighbor_threshold(P.h[r]);
+        P.mass[r] = c.fluid_particle_mass[r];
+        P.poly6[r] = (float)(315.0 / (64.0 * pi * h3 * h3 * h3));
+        P.spiky[r] = (float)(45.0 / (pi * h3 * h3));
+    }
+    const double m0 = c.fluid_particle_mass[0], mb = c.boundary_particle_mass;
+    P.rho0 = c.rest_density;
+    P.bulk = c.bulk_modulus;
+    P.mu = c.viscosity;
+    P.sigma = c.tension_coefficient;
+    P.bnd_coef = (float)(0.02 * (double)c.speed_sound * c.speed_sound * mb / (m0 + mb));
+    P.two_over_h0 = (float)(2.0 / (double)c.effective_radius[0]);
+    P.gravity = -9.81f;
+    P.blend_inc = c.blend_increment;
+    P.axis = c.refine_axis;
+    P.lo = c.refine_lo;
+    P.hi = c.refine_hi;
+    P.lo43 = std::llrint((double)c.refine_lo * 8796093022208.0);
+    P.hi43 = std::llrint((double)c.refine_hi * 8796093022208.0);
+    *out = P;
+    return SPH_OK;
+}
+
+int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, std::vector<void*>& o) {
+    p.cap = cap;
+    p.ncells = sph_grid_num_cells(&g);
+    p.key_bits = 3 * morton_bits_for(g);
+    int rc = SPH_OK;
+    if ((rc = dalloc(&p.pos, cap, o)) || (rc = dalloc(&p.vel, cap, o)) ||
+        (rc = dalloc(&p.stt, cap, o)) || (rc = dalloc(&p.grp, cap, o)) ||
+        (rc = dalloc(&p.spos, cap, o)) || (rc = dalloc(&p.svel, cap, o)) ||
+        (rc = dalloc(&p.sstt, cap, o)) || (rc = dalloc(&p.sgrp, cap, o)) ||
+        (rc = dalloc(&p.rho, cap, o)) || (rc = dalloc(&p.aux, cap, o)) ||
+        (rc = dalloc(&p.ipos, cap, o)) || (rc = dalloc(&p.ivel, cap, o)) ||
+        (rc = dalloc(&p.istt, cap, o)) || (rc = dalloc(&p.igrp, cap, o)) ||
+        (rc = dalloc(&p.keep, cap, o)) || (rc = dalloc(&p.off, cap, o)) ||
+        (rc = dalloc(&p.split, cap, o)) || (rc = dalloc(&p.soff, cap, o)) ||
+        (rc = dalloc(&p.cells, p.ncells, o)))
+        return rc;
+    return SPH_OK;
+}
+
+TSOut outputs(Pop& p, float* acc, uint32_t* nbr_bnd) {
+    TSOut o;
+    o.ipos = p.ipos;
+    o.ivel = p.ivel;
+    o.istt = p.istt;
+    o.igrp = p.igrp;
+    o.keep = p.keep;
+    o.split = p.split;
+    o.acc = acc;
+    o.nbr_bnd = nbr_bnd;
+    return o;
+}
+
+// hash -> sort -> reorder + cell ranges of population r (Solver.cu:1616-1680).
+void ts_neighborhood(sph_solver2* s, int r) {
+    Pop& p = s->pop[r];
+    cudaStream_t st = s->stream;
+    cudaMemsetAsync(p.cells, 0xFF, sizeof(uint2) * p.ncells, st);
+    if (p.n == 0) return;
+    const int passes = sort_passes(p.key_bits);
+    sort_reset(s->sort, st);
+    uint32_t hb = blocks_for(p.n);
+    if (hb > 1216) hb = 1216;
+    hash_hist_kernel<<<hb, 256, 0, st>>>(p.pos, p.n, s->P.g[r], passes, s->keys[0], s->sort.hist);
+    sort_scan(passes, s->sort, st);
+    const int o = sort_passes_run(s->keys, s->vals, nullptr, p.n, passes, s->sort, s->err, 0, st);
+    if (r == 1)
+        ts_gather_kernel<true><<<blocks_for(p.n), 256, 0, st>>>(
+            s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
+            p.sstt, p.sgrp, p.cells, s->err, s->P.axis, s->group_base, s->gsum, s->gready);
+    else
+        ts_gather_kernel<false><<<blocks_for(p.n), 256, 0, st>>>(
+            s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
+            p.sstt, p.sgrp, p.cells, s->err, -1, 0, nullptr, nullptr);
+}
+
+// Everything up to and including the force/integrate pass; DEBUG variants
+// also write accelerations and neighbour counts of population `dbg_pop`.
+void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_same,
+              uint32_t* dnb_compl, float* dacc, uint32_t* dnb_bnd) {
+    cudaStream_t st = s->stream;
+    const uint32_t gb = s->group_base;
+    if (gb) {
+        cudaMemsetAsync(s->gsum, 0, 8 * (size_t)gb, st);
+        cudaMemsetAsync(s->gready, 0, 4 * (size_t)gb, st);
+        cudaMemsetAsync(s->gacc, 0, 48 * (size_t)gb, st);
+    }
+    cudaMemsetAsync(s->ctl + kCtlFadedL, 0, 8, st);
+    ts_neighborhood(s, 1);
+    ts_neighborhood(s, 0);
+    if (gb && s->P.axis >= 0)
+        ts_group_decide_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gsum, s->gready, gb, s->P.lo43,
+                                                               s->P.hi43, s->gmerge);
+    else if (gb)
+        cudaMemsetAsync(s->gmerge, 0, 4 * (size_t)gb, st);
+    Pop &L = s->pop[0], &H = s->pop[1];
+    if (H.n) {
+        if (debug && dbg_pop == 1)
+            ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
+                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, dnb_same, dnb_compl);
+        else
+            ts_density_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
+                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, nullptr, nullptr);
+    }
+    if (L.n) {
+        if (debug && dbg_pop == 0)
+            ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
+                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl);
+        else
+            ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
+                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr);
+    }
+    const uint32_t* gm = gb ? s->gmerge : nullptr;
+    if (H.n) {
+        TSOut o = outputs(H, dacc, dnb_bnd);
+        if (debug && dbg_pop == 1)
+            ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
+                H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+        else
+            ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
+                H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+    }
+    if (L.n) {
+        TSOut o = outputs(L, dacc, dnb_bnd);
+        if (debug && dbg_pop == 0)
+            ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
+                L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+        else
+            ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
+                L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+    }
+}
+
+int check_err2(sph_solver2* s) {
+    uint32_t e = 0;
+    SPH_CUDA(cudaMemcpyAsync(&e, s->err, 4, cudaMemcpyDeviceToHost, s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (e) {
+        SPH_CUDA(cudaMemsetAsync(s->err, 0, 4, s->stream));
+        SPH_CUDA(cudaStreamSynchronize(s->stream));
+        if (e & kErrLookbackTimeout)
+            return fail(SPH_E_TIMEOUT, "radix sort look-back timed out; step results are invalid");
+        if (e & 4u)
+            return fail(SPH_E_CAPACITY, "two-scale step exceeded a particle or group capacity");
+        return fail(SPH_E_CAPACITY, "device-side index check failed");
+    }
+    return SPH_OK;
+}
+
+int ts_step(sph_solver2* s, float dt) {
+    cudaStream_t st = s->stream;
+    Pop &L = s->pop[0], &H = s->pop[1];
+    const uint32_t gb = s->group_base;
+    ts_front(s, dt, false, 0, nullptr, nullptr, nullptr, nullptr);
+    // compaction (prefix sums over keep / split / merge flags)
+    if (H.n) scan_exclusive(H.keep, H.off, H.n, s->scan_scratch, s->tot + 0, st);
+    if (L.n) {
+        scan_exclusive(L.keep, L.off, L.n, s->scan_scratch, s->tot + 1, st);
+        scan_exclusive(L.split, L.soff, L.n, s->scan_scratch, s->tot + 2, st);
+    }
+    scan_exclusive(s->gmerge, s->moff, gb, s->scan_scratch, s->tot + 3, st);
+    ts_totals_kernel<<<1, 1, 0, st>>>(s->tot, H.n, L.n, H.cap, L.cap, s->cap_groups, s->ctl, s->err);
+    if (H.n)
+        ts_compact_kernel<<<blocks_for(H.n), 256, 0, st>>>(outputs(H, nullptr, nullptr), H.off, H.n,
+                                                           H.cap, H.pos, H.vel, H.stt, H.grp);
+    if (L.n) {
+        ts_compact_kernel<<<blocks_for(L.n), 256, 0, st>>>(outputs(L, nullptr, nullptr), L.off, L.n,
+                                                           L.cap, L.pos, L.vel, L.stt, L.grp);
+        ts_children_kernel<<<blocks_for(L.n), 256, 0, st>>>(
+            outputs(L, nullptr, nullptr), L.soff, L.rho, L.n, s->P.mass[0], s->ctl, H.cap, H.pos,
+            H.vel, H.stt, H.grp);
+    }
+    if (gb)
+        ts_merge_spawn_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gmerge, s->moff, s->gacc, gb,
+                                                              s->ctl, L.cap, L.pos, L.vel, L.stt,
+                                                              L.grp);
+    ts_advance_counters_kernel<<<1, 1, 0, st>>>(s->ctl, s->cap_groups);
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaMemcpyAsync(s->ctl_host, s->ctl, 4 * kCtlWords, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(cudaStreamSynchronize(st));
+    const uint32_t* c = s->ctl_host;
+    s->stats[0] = c[kCtlSplits];
+    s->stats[1] = c[kCtlMerges];
+    s->stats[2] = L.n - c[kCtlSurvL];
+    s->stats[3] = H.n - c[kCtlSurvH];
+    s->stats[4] = c[kCtlFadedL];
+    s->stats[5] = c[kCtlFadedH];
+    H.n = c[kCtlNextH];
+    L.n = c[kCtlNextL];
+    s->group_base = c[kCtlGroupBase];
+    s->next_id[0] = c[kCtlPidL];
+    s->next_id[1] = c[kCtlPidH];
+    return check_err2(s);
+}
+
+int upload_pop(sph_solver2* s, int r, const float* xyz, uint32_t n) {
+    Pop& p = s->pop[r];
+    std::vector<float4> hp(n), hv(n);
+    std::vector<int32_t> hs(n, r == 1 ? 4 : 0);  // HIGH states start at 4 (Solver.cu:1537-1543)
+    std::vector<uint32_t> hg(n, kNoGroup);
+    for (uint32_t i = 0; i < n; ++i) {
+        float w;
+        std::memcpy(&w, &i, 4);
+        hp[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], w);
+        hv[i] = make_float4(0.f, 0.f, 0.f, 1.0f);  // lambda starts at 1 (Solver.cu:1371)
+    }
+    if (n) {
+        SPH_CUDA(cudaMemcpy(p.pos, hp.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.vel, hv.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.stt, hs.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.grp, hg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+    }
+    p.n = n;
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// SolverConfiguration::MakeConfiguration of the two-scale project
+// (SPH2S_FINAL_TWO_SCALE/Solver.h:16-50): h1 = h0/2, m1 = m0/8, one grid per
+// radius; refinement disabled (refine_axis = -1).
+int sph_make_configuration2(const float origin[3], const float end[3], float volume,
+                            uint32_t num_particles, uint32_t avg_particles, float rest_density,
+                            float bulk_modulus, float viscosity, float speed_sound,
+                            float tension_coefficient, float blend_increment, sph_config2* out) {
+    if (!out) return fail(SPH_E_INVALID, "sph_make_configuration2: NULL output");
+    sph_config c1;
+    int rc = sph_make_configuration(origin, end, volume, num_particles, avg_particles,
+                                    rest_density, bulk_modulus, viscosity, speed_sound,
+                                    tension_coefficient, 0.0f, &c1);
+    if (rc != SPH_OK) return rc;
+    sph_config2 c;
+    std::memset(&c, 0, sizeof(c));
+    c.effective_radius[0] = c1.effective_radius;
+    c.effective_radius[1] = 0.5f * c1.effective_radius;
+    c.fluid_particle_mass[0] = c1.fluid_particle_mass;
+    c.fluid_particle_mass[1] = 1.0f / 8.0f * c1.fluid_particle_mass;
+    c.boundary_particle_mass = c1.fluid_particle_mass;
+    c.rest_density = rest_density;
+    c.bulk_modulus = bulk_modulus;
+    c.viscosity = viscosity;
+    c.speed_sound = speed_sound;
+    c.tension_coefficient = tension_coefficient;
+    c.blend_increment = blend_increment;
+    c.grid[0] = c1.grid;
+    rc = sph_make_grid(origin, end, c.effective_radius[1], &c.grid[1]);
+    if (rc != SPH_OK) return rc;
+    c.refine_axis = -1;
+    *out = c;
+    return SPH_OK;
+}
+
+int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
+                const float* high_xyz, uint32_t n_high, const float* boundary_xyz,
+                uint32_t n_boundary, uint32_t capacity_low, uint32_t capacity_high,
+                sph_solver2** out) {
+    if (!config || !out) return fail(SPH_E_INVALID, "sph2_create: NULL config or output handle");
+    *out = nullptr;
+    if ((n_low && !low_xyz) || (n_high && !high_xyz) || (n_boundary && !boundary_xyz))
+        return fail(SPH_E_INVALID, "sph2_create: NULL particle array");
+    TSParams P;
+    int rc = make_ts_params(*config, &P);
+    if (rc != SPH_OK) return rc;
+    uint64_t capL = capacity_low ? capacity_low : 2ull * n_low + 1024;
+    uint64_t capH = capacity_high ? capacity_high : 8ull * (n_low + n_high) + 1024;
+    if (capL < n_low || capH < n_high) return fail(SPH_E_CAPACITY, "sph2_create: capacity below the initial count");
+    if (capL > kMaxParticles || capH > kMaxParticles || n_boundary > kMaxParticles)
+        return fail(SPH_E_CAPACITY, "sph2_create: more than 2^30 particles");
+    sph_solver2* s = new sph_solver2();
+    s->cfg = *config;
+    s->P = P;
+    s->nb = n_boundary;
+    s->next_id[0] = n_low;
+    s->next_id[1] = n_high;
+    s->cap_groups = (uint32_t)(capH / 8 * 4 + 64);
+#define TRY(x)                                 \
+    do {                                       \
+        int _r = (x);                          \
+        if (_r != SPH_OK) {                    \
+            std::string m = sph_last_error();  \
+            free_solver2(s);                   \
+            return fail(_r, m);                \
+        }                                      \
+    } while (0)
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], s->owned));
+    TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], s->owned));
+    const uint32_t nmax = (uint32_t)std::max<uint64_t>(std::max(capL, capH), n_boundary);
+    for (int b = 0; b < 2; ++b) {
+        TRY(dalloc(&s->keys[b], nmax, s->owned));
+        TRY(dalloc(&s->vals[b], nmax, s->owned));
+    }
+    TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
+    s->owned.push_back(s->sort_mem);
+    s->sort = sort_scratch_from(s->sort_mem, nmax);
+    TRY(dalloc(&s->scan_scratch, scan_scratch_words(std::max<uint32_t>(nmax, s->cap_groups)), s->owned));
+    TRY(dalloc(&s->tot, 4, s->owned));
+    TRY(dalloc(&s->gsum, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gready, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gmerge, s->cap_groups, s->owned));
+    TRY(dalloc(&s->moff, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gacc, 6 * (size_t)s->cap_groups, s->owned));
+    TRY(dalloc(&s->ctl, kCtlWords, s->owned));
+    TRY(dalloc(&s->err, 1, s->owned));
+    TRY(dalloc(&s->bpos, n_boundary, s->owned));
+    TRY(dalloc(&s->bcells, s->pop[0].ncells, s->owned));
+    TRY(check_cuda(cudaMallocHost((void**)&s->ctl_host, 4 * kCtlWords), "pinned", __FILE__, __LINE__));
+    TRY(check_cuda(cudaMemset(s->err, 0, 4), "memset", __FILE__, __LINE__));
+    {
+        uint32_t c0[kCtlWords] = {0};
+        c0[kCtlPidH] = n_high;
+        c0[kCtlPidL] = n_low;
+        TRY(check_cuda(cudaMemcpy(s->ctl, c0, sizeof(c0), cudaMemcpyHostToDevice), "ctl", __FILE__, __LINE__));
+    }
+    for (int b = 0; b < 2; ++b) {
+        TRY(check_cuda(cudaMemset(s->keys[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
+        TRY(check_cuda(cudaMemset(s->vals[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
+    }
+    TRY(upload_pop(s, 0, low_xyz, n_low));
+    TRY(upload_pop(s, 1, high_xyz, n_high));
+    // boundary: sorted once on the LOW grid (SPH2S_FINAL_TWO_SCALE/Solver.cu:1469-1527)
+    TRY(check_cuda(cudaMemset(s->bcells, 0xFF, sizeof(uint2) * s->pop[0].ncells), "memset", __FILE__, __LINE__));
+    if (n_boundary) {
+        std::vector<float4> hb(n_boundary);
+        for (uint32_t i = 0; i < n_boundary; ++i) {
+            float w;
+            std::memcpy(&w, &i, 4);
+            hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
+        }
+        float4* braw = nullptr;
+        cudaError_t e = cudaMalloc(&braw, 16 * (size_t)n_boundary);
+        if (e == cudaSuccess) e = cudaMemcpy(braw, hb.data(), 16 * (size_t)n_boundary, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            const int passes = sort_passes(s->pop[0].key_bits);
+            sort_reset(s->sort, s->stream);
+            uint32_t hbk = blocks_for(n_boundary);
+            if (hbk > 1216) hbk = 1216;
+            hash_hist_kernel<<<hbk, 256, 0, s->stream>>>(braw, n_boundary, s->P.g[0], passes,
+                                                         s->keys[0], s->sort.hist);
+            sort_scan(passes, s->sort, s->stream);
+            const int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort,
+                                          s->err, 0, s->stream);
+            gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
+                s->keys[o], s->vals[o], n_boundary, s->P.g[0], braw, nullptr, s->bpos, nullptr,
+                s->bcells, s->err);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        }
+        if (braw) cudaFree(braw);
+        TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
+    }
+    TRY(check_err2(s));
+#undef TRY
+    *out = s;
+    return SPH_OK;
+}
+
+int sph2_advance(sph_solver2* s, float dt, int32_t steps) {
+    if (!s) return fail(SPH_E_INVALID, "sph2_advance: NULL handle");
+    if (steps < 0 || !(dt > 0.0f) || !std::isfinite(dt))
+        return fail(SPH_E_INVALID, "sph2_advance: bad dt or steps");
+    for (int k = 0; k < steps; ++k) {
+        int rc = ts_step(s, dt);
+        if (rc != SPH_OK) return rc;
+    }
+    return SPH_OK;
+}
+
+int sph2_counts(sph_solver2* s, uint32_t* n_low, uint32_t* n_high, uint32_t* n_boundary,
+                uint32_t* groups) {
+    if (!s) return fail(SPH_E_INVALID, "sph2_counts: NULL handle");
+    if (n_low) *n_low = s->pop[0].n;
+    if (n_high) *n_high = s->pop[1].n;
+    if (n_boundary) *n_boundary = s->nb;
+    if (groups) *groups = s->group_base;
+    return SPH_OK;
+}
+
+int sph2_next_ids(sph_solver2* s, uint32_t* next_low, uint32_t* next_high) {
+    if (!s) return fail(SPH_E_INVALID, "sph2_next_ids: NULL handle");
+    if (next_low) *next_low = s->next_id[0];
+    if (next_high) *next_high = s->next_id[1];
+    return SPH_OK;
+}
+
+int sph2_last_stats(sph_solver2* s, uint32_t* stats) {
+    if (!s || !stats) return fail(SPH_E_INVALID, "sph2_last_stats: NULL argument");
+    std::memcpy(stats, s->stats, sizeof(s->stats));
+    return SPH_OK;
+}
+
+int sph2_get_state(sph_solver2* s, int32_t population, float* xyz, float* vel, float* lambda,
+                   int32_t* state, uint32_t* group, uint32_t* ids) {
+    if (!s || population < 0 || population > 1)
+        return fail(SPH_E_INVALID, "sph2_get_state: bad handle or population");
+    Pop& p = s->pop[population];
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    const uint32_t n = p.n;
+    std::vector<float4> hp(n), hv(n);
+    if (n) {
+        SPH_CUDA(cudaMemcpy(hp.data(), p.pos, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+        SPH_CUDA(cudaMemcpy(hv.data(), p.vel, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+        if (state) SPH_CUDA(cudaMemcpy(state, p.stt, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+        if (group) SPH_CUDA(cudaMemcpy(group, p.grp, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        if (xyz) {
+            xyz[3 * i] = hp[i].x;
+            xyz[3 * i + 1] = hp[i].y;
+            xyz[3 * i + 2] = hp[i].z;
+        }
+        if (vel) {
+            vel[3 * i] = hv[i].x;
+            vel[3 * i + 1] = hv[i].y;
+            vel[3 * i + 2] = hv[i].z;
+        }
+        if (lambda) lambda[i] = hv[i].w;
+        if (ids) std::memcpy(&ids[i], &hp[i].w, 4);
+    }
+    return SPH_OK;
+}
+
+int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sorted, float* rho,
+                           float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
+                           uint32_t* nbr_boundary) {
+    if (!s || population < 0 || population > 1)
+        return fail(SPH_E_INVALID, "sph2_debug_step_fields: bad handle or population");
+    Pop& p = s->pop[population];
+    const uint32_t n = p.n;
+    if (n == 0) return SPH_OK;
+    float* dacc = nullptr;
+    uint32_t *ds = nullptr, *dc = nullptr, *db = nullptr;
+    SPH_CUDA(cudaMalloc(&dacc, 12 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&ds, 4 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&dc, 4 * (size_t)n));
+    SPH_CUDA(cudaMalloc(&db, 4 * (size_t)n));
+    ts_front(s, 1e-6f, true, population, ds, dc, dacc, db);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    std::vector<float4> sv;
+    if (e == cudaSuccess && ids_sorted) {
+        sv.resize(n);
+        e = cudaMemcpy(sv.data(), p.svel, 16 * (size_t)n, cudaMemcpyDeviceToHost);
+        for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) std::memcpy(&ids_sorted[i], &sv[i].w, 4);
+    }
+    if (e == cudaSuccess && rho) e = cudaMemcpy(rho, p.rho, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && acc) e = cudaMemcpy(acc, dacc, 12 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nbr_same) e = cudaMemcpy(nbr_same, ds, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nbr_compl) e = cudaMemcpy(nbr_compl, dc, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nbr_boundary) e = cudaMemcpy(nbr_boundary, db, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(dacc);
+    cudaFree(ds);
+    cudaFree(dc);
+    cudaFree(db);
+    SPH_CUDA(e);
+    return check_err2(s);
+}
+
+int sph2_destroy(sph_solver2* s) { return free_solver2(s); }
+
+}  // extern "C"

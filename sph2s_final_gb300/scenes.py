@@ -70,3 +70,37 @@ def dam_break(spacing: float, fluid_dims=None, seed: int = 0, jitter_amount: flo
 def small_scene(k: int = 8, seed: int = 0) -> Scene:
     """A k^3 block at spacing 1/(2k) in the unit box (fast parity cases)."""
     return dam_break(0.5 / k, (k, k, k), seed=seed, dt=1e-4)
+
+
+@dataclass
+class TwoScaleScene:
+    low: ParticleData
+    boundary: ParticleData
+    config: object
+    dt: float
+    spacing: float
+
+
+def two_scale_dam_break(spacing: float = 1 / 128, fluid_dims=None, seed: int = 0,
+                        jitter_amount: float = 0.01, slab=(0.35, 0.65), axis: int = 0,
+                        blend_increment: float = 0.0125, dt: float = 2.5e-5,
+                        border: int = 5) -> TwoScaleScene:
+    """Coarse dam break with a refinement slab: LOW support h = 2s, mass
+    1000 s^3; HIGH support h/2, mass m/8; LOW grid spacing h, HIGH grid h/2
+    over the unit box; slab lo < x[axis] < hi drives split and merge."""
+    from .two_scale import SolverConfiguration2
+    s = float(np.float32(spacing))
+    if fluid_dims is None:
+        k = int(round(0.5 / s))
+        fluid_dims = (k, k, k)
+    low = jitter(lattice_block(s, fluid_dims), s, jitter_amount, seed)
+    box = Grid.make_grid((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), s)
+    boundary = ParticleData.create_particle_box_canvas(box, border)
+    h = float(np.float32(2.0 * s))
+    g0 = Grid.make_grid((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), h)
+    g1 = Grid.make_grid((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), float(np.float32(0.5) * np.float32(h)))
+    mass = float(np.float32(REST_DENSITY * s ** 3))
+    cfg = SolverConfiguration2.direct(h, mass, REST_DENSITY, BULK_MODULUS, VISCOSITY, SPEED_SOUND,
+                                      TENSION, blend_increment, g0, g1, refine_axis=axis,
+                                      refine_lo=slab[0], refine_hi=slab[1])
+    return TwoScaleScene(ParticleData(low), boundary, cfg, dt, s)
