@@ -212,6 +212,44 @@ int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sor
                            uint32_t* nbr_boundary);
 int sph2_destroy(sph_solver2* s);
 
+/* ---- batched single-scale scenes --------------------------------------- */
+
+/* One scene of a batch: its own particles, boundary and configuration (grid,
+ * h, masses, viscosity, stiffness may all differ between scenes). */
+typedef struct sph_scene_desc {
+    const float* fluid_xyz;
+    uint32_t n_fluid;
+    const float* boundary_xyz;
+    uint32_t n_boundary;
+    const float* velocity_xyz; /* NULL = zero */
+    sph_config config;
+} sph_scene_desc;
+
+typedef struct sph_batch sph_batch;
+
+/* Many independent Solver instances stepped together.  The reference can
+ * step only one solver at a time (one bound __constant__ configuration,
+ * SPH2S_FINAL_SINGLE_SCALE/Solver.cu:12, 1068-1080); a batch packs the
+ * scenes and advances all of them with one launch per kernel, each step one
+ * CUDA graph.  Every scene evolves exactly as sph_create/sph_advance would
+ * evolve it alone. */
+int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** out);
+int sphb_advance(sph_batch* b, float dt, int32_t steps);
+int sphb_sync(sph_batch* b);
+void* sphb_stream(sph_batch* b);
+int sphb_counts(sph_batch* b, uint32_t* num_scenes, uint32_t* total_fluid,
+                uint32_t* total_boundary);
+/* Positions, velocities (3 floats per particle) and densities of one scene,
+ * sorted order or by the scene-local creation index; each pointer optional. */
+int sphb_get_scene(sph_batch* b, uint32_t scene, float* xyz, float* vel, float* rho,
+                   int32_t order);
+/* Times block sizes 128/256/512 for the density and force passes and 2/4/8
+ * resident blocks per SM for the persistent grid on the batch's own data,
+ * keeps the fastest (choice3 = density block, force block, blocks per SM),
+ * and restores the particle state. */
+int sphb_autotune(sph_batch* b, float dt, int32_t* choice3);
+int sphb_destroy(sph_batch* b);
+
 /* ---- key-value sort ------------------------------------------------------ */
 
 /* Stable ascending sort of n (uint32 key, uint32 value) pairs in device

@@ -66,6 +66,17 @@ class sph_config2(C.Structure):
     ]
 
 
+class sph_scene_desc(C.Structure):
+    _fields_ = [
+        ("fluid_xyz", C.POINTER(C.c_float)),
+        ("n_fluid", C.c_uint32),
+        ("boundary_xyz", C.POINTER(C.c_float)),
+        ("n_boundary", C.c_uint32),
+        ("velocity_xyz", C.POINTER(C.c_float)),
+        ("config", sph_config),
+    ]
+
+
 _f = C.POINTER(C.c_float)
 _u = C.POINTER(C.c_uint32)
 _vp = C.c_void_p
@@ -106,6 +117,14 @@ SIGNATURES = {
     "sph2_get_state": (C.c_int, [_vp, C.c_int32, _f, _f, _f, C.POINTER(C.c_int32), _u, _u]),
     "sph2_debug_step_fields": (C.c_int, [_vp, C.c_int32, _u, _f, _f, _u, _u, _u]),
     "sph2_destroy": (C.c_int, [_vp]),
+    "sphb_create": (C.c_int, [C.POINTER(sph_scene_desc), C.c_uint32, C.POINTER(_vp)]),
+    "sphb_advance": (C.c_int, [_vp, C.c_float, C.c_int32]),
+    "sphb_sync": (C.c_int, [_vp]),
+    "sphb_stream": (C.c_void_p, [_vp]),
+    "sphb_counts": (C.c_int, [_vp, _u, _u, _u]),
+    "sphb_get_scene": (C.c_int, [_vp, C.c_uint32, _f, _f, _f, C.c_int32]),
+    "sphb_autotune": (C.c_int, [_vp, C.c_float, C.POINTER(C.c_int32)]),
+    "sphb_destroy": (C.c_int, [_vp]),
     "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -27,13 +27,16 @@ namespace sph {
 
 constexpr int kDensityThreads = 256;
 
+// Density of particle i of the sorted array (n particles, indices in `cells`
+// refer to that array); the batched solver calls this with per-scene P and
+// cell table.
 template <bool DEBUG>
-__global__ void __launch_bounds__(kDensityThreads) density_kernel(
-    const float4* __restrict__ pos, const uint2* __restrict__ cells, uint32_t n, SimParams P,
-    float* __restrict__ rho, float2* __restrict__ aux, uint4* __restrict__ nbr4,
-    uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ dbg_count) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void density_one(uint32_t i, const float4* __restrict__ pos,
+                                            const uint2* __restrict__ cells, uint32_t n,
+                                            const SimParams& P, float* __restrict__ rho,
+                                            float2* __restrict__ aux, uint4* __restrict__ nbr4,
+                                            uint32_t* __restrict__ nbr_count,
+                                            uint32_t* __restrict__ dbg_count) {
     uint32_t k = 0, zero = 0;
     uint4 buf = make_uint4(0u, 0u, 0u, 0u);
     float sum = 0.0f;
@@ -76,6 +79,16 @@ __global__ void __launch_bounds__(kDensityThreads) density_kernel(
     aux[i] = make_float2(p * inv * inv, inv);
     nbr_count[i] = k;
     if (DEBUG) dbg_count[i] = k + zero;
+}
+
+template <bool DEBUG>
+__global__ void __launch_bounds__(kDensityThreads) density_kernel(
+    const float4* __restrict__ pos, const uint2* __restrict__ cells, uint32_t n, SimParams P,
+    float* __restrict__ rho, float2* __restrict__ aux, uint4* __restrict__ nbr4,
+    uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ dbg_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    density_one<DEBUG>(i, pos, cells, n, P, rho, aux, nbr4, nbr_count, dbg_count);
 }
 
 }  // namespace sph

@@ -33,16 +33,16 @@ __device__ __forceinline__ void force_pair(ForceAcc& A, const SimParams& P, floa
 // Pressure (spiky gradient), viscosity (Laplacian), tension (Poly6), boundary
 // force and gravity; MODE 0 integrates (symplectic Euler) into pos_out/vel_out,
 // MODE 1 writes the acceleration and the boundary neighbour count instead.
+// Particle i of the sorted array; cells/bcells/bnear are the particle's own
+// grid tables (the batched solver passes per-scene tables and P).
 template <int MODE>
-__global__ void __launch_bounds__(256) force_kernel(
-    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ aux,
-    const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
+__device__ __forceinline__ void force_one(
+    uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel,
+    const float2* __restrict__ aux, const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
-    SimParams P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+    const SimParams& P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
     float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const float4 xi = pos[i];
     const float4 vi = vel[i];
     const float2 ai = aux[i];
@@ -128,6 +128,20 @@ __global__ void __launch_bounds__(256) force_kernel(
         acc_out[3 * i + 2] = azz;
         nbr_b[i] = bcnt;
     }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) force_kernel(
+    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ aux,
+    const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
+    const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
+    const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
+    SimParams P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    force_one<MODE>(i, pos, vel, aux, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P, dt,
+                    pos_out, vel_out, acc_out, nbr_b);
 }
 
 }  // namespace sph

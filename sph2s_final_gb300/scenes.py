@@ -104,3 +104,24 @@ def two_scale_dam_break(spacing: float = 1 / 128, fluid_dims=None, seed: int = 0
                                       TENSION, blend_increment, g0, g1, refine_axis=axis,
                                       refine_lo=slab[0], refine_hi=slab[1])
     return TwoScaleScene(ParticleData(low), boundary, cfg, dt, s)
+
+
+def batched_scenes(num: int = 256, seed: int = 2, n_min: int = 4096, n_max: int = 131072,
+                   dt: float = 5e-5):
+    """Independent dam breaks with log-uniform particle counts in [n_min, n_max]:
+    lattice side k = round(n^(1/3)) in [0, 0.5]^3 at s = 0.5/k, h = 2s, each in
+    its own unit box and grid; viscosity and stiffness scaled per scene by
+    U[0.5, 2].  One dt for all scenes (5e-5 keeps dt/s <= 6.4e-3, the ratio of
+    the 32^3 and 128^3 single-scale cases, down to the finest scene)."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(n_min), np.log(n_max), num))
+    mu_scale = rng.uniform(0.5, 2.0, num)
+    k_scale = rng.uniform(0.5, 2.0, num)
+    out = []
+    for i in range(num):
+        k = int(round(n[i] ** (1.0 / 3.0)))
+        sc = dam_break(0.5 / k, (k, k, k), seed=seed * 100003 + i, dt=dt,
+                       viscosity=VISCOSITY * float(mu_scale[i]),
+                       bulk_modulus=BULK_MODULUS * float(k_scale[i]))
+        out.append(sc)
+    return out
