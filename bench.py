@@ -46,6 +46,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile-steps", type=int, default=200)
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint measurements")
+    ap.add_argument("--batched-steps", type=int, default=500)
     return ap.parse_args()
 
 
@@ -188,6 +190,55 @@ def cpu_baseline(sc, seconds: float):
             "sample": f"FP64 oracle (C++/OpenMP) on the same scene, {steps} steps after 1 warm-up step"}
 
 
+def measure_batched(steps: int, warmup: int = 3):
+    """256 independent scenes (9.4M fluid particles): one batch stepped with one
+    launch per kernel per step, against the same scenes stepped one after
+    another by per-scene solvers (each with its own CUDA graph)."""
+    import torch
+
+    from sph2s_final_gb300 import scenes
+    from sph2s_final_gb300.batched import Batch
+    from sph2s_final_gb300.solver import Solver
+
+    scs = scenes.batched_scenes()
+    dt = scs[0].dt
+    items = [(s.fluid.positions, s.boundary.positions, s.config) for s in scs]
+    n = sum(s.fluid.num_particles for s in scs)
+    with Batch(items) as b:
+        choice = b.autotune(dt)
+        b.advance(dt, warmup)
+        b.sync()
+        st = torch.cuda.ExternalStream(b.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        b.advance(dt, steps)
+        e1.record(st)
+        b.sync()
+        batched_ms = e0.elapsed_time(e1)
+    solvers = [Solver(s.fluid, s.boundary, s.config) for s in scs]
+    for s in solvers:
+        s.advance(dt, warmup)
+        s.sync()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.advance(dt, steps)
+        s.sync()
+    serial_ms = 1e3 * (time.perf_counter() - t0)
+    for s in solvers:
+        s.close()
+    return {"scenes": len(scs), "fluid_particles": n, "steps": steps, "dt": dt,
+            "batched_ms": batched_ms, "per_scene_serial_ms": serial_ms,
+            "speedup": serial_ms / batched_ms,
+            "batched_particle_steps_per_s": n * steps / (batched_ms * 1e-3),
+            "per_scene_particle_steps_per_s": n * steps / (serial_ms * 1e-3),
+            "autotune": choice,
+            "timing": "batched: CUDA events on the batch stream; per-scene: host clock, "
+                      "each scene synchronised before the next starts"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -326,6 +377,8 @@ def run_ours(args):
     }
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds)
+    if ws == 1 and not args.no_extras:
+        line["batched"] = measure_batched(args.batched_steps)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
