@@ -141,6 +141,28 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms);
  * bounded spin, so the next sph_sync returns SPH_E_TIMEOUT without hanging. */
 int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on);
 
+/* ---- differentiable rollout (no counterpart in the reference) ------------ */
+
+/* Restarts the solver from its creation positions with initial velocities
+ * v0 (3 floats per particle in creation order, NULL = zero) and viscosity
+ * `viscosity`, and runs `steps` steps of dt, checkpointing the state every
+ * `checkpoint_every` steps for the backward pass. */
+int sph_rollout_forward(sph_solver* s, const float* v0_xyz, float viscosity, float dt,
+                        int32_t steps, int32_t checkpoint_every);
+/* Poly6 splat G of the current particles on the cell centres of `nodes`
+ * (G_n = m sum_i W(|y_n - x_i|), the density pass's kernel and stencil rule);
+ * `field` (optional) receives G.  With a target (one value per node),
+ * *loss = mean_n (G_n - target_n)^2 and, after sph_rollout_forward, its
+ * gradient with respect to the final positions is kept for the backward. */
+int sph_rollout_density_loss(sph_solver* s, const sph_grid* nodes, const float* target,
+                             float* field, double* loss);
+/* Reverse pass of the last forward + loss: hand-written adjoints of
+ * integrate, force and density, recomputing each checkpoint segment and
+ * holding every step's neighbour structure constant.  Gradients with respect
+ * to the initial velocities and positions (3 floats per particle, creation
+ * order; each optional) and the viscosity. */
+int sph_rollout_backward(sph_solver* s, float* grad_v0, float* grad_x0, double* grad_mu);
+
 /* ---- two-scale solver -------------------------------------------------- */
 
 #define SPH_LOW 0  /* coarse population: support h, mass m */

@@ -143,3 +143,33 @@ class SSRollout:
             self.close()
         except Exception:
             pass
+
+
+def splat_loss(config, x, nodes_dims=(32, 32, 32), target=None):
+    """FP64 Poly6 splat of positions x (n,3) on the cell centres of a grid over
+    the unit box (G_n = m sum_i W(|y_n - x_i|), r < h), and the mean squared
+    error against `target` if given.  Test infrastructure for finite
+    differences of the differentiable rollout."""
+    x = np.asarray(x, np.float64)
+    h = float(np.float32(config.effective_radius))
+    m = float(np.float32(config.fluid_particle_mass))
+    c6 = 315.0 / (64.0 * np.pi * h ** 9)
+    d = np.array(nodes_dims)
+    sp = 1.0 / d[0]
+    base = np.floor(x / sp - 0.5).astype(np.int64)
+    field = np.zeros(int(np.prod(d)))
+    offs = np.arange(-1, 3)
+    for ox in offs:
+        for oy in offs:
+            for oz in offs:
+                idx = base + np.array([ox, oy, oz])
+                ok = np.all((idx >= 0) & (idx < d), axis=1)
+                y = (idx + 0.5) * sp
+                r2 = ((x - y) ** 2).sum(1)
+                w = np.where(ok & (r2 < h * h), (h * h - r2) ** 3, 0.0)
+                lin = idx[:, 0] + d[0] * (idx[:, 1] + d[1] * idx[:, 2])
+                np.add.at(field, lin[ok], w[ok])
+    field *= m * c6
+    if target is None:
+        return field, None
+    return field, float(((field - np.asarray(target, np.float64)) ** 2).mean())

@@ -105,6 +105,10 @@ SIGNATURES = {
     "sph_debug_step_fields": (C.c_int, [_vp, _u, _u, _u, _u, _u, _u, _f, _f]),
     "sph_profile_phases": (C.c_int, [_vp, C.c_float, C.c_int32, _f]),
     "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
+    "sph_rollout_forward": (C.c_int, [_vp, _f, C.c_float, C.c_float, C.c_int32, C.c_int32]),
+    "sph_rollout_density_loss": (C.c_int, [_vp, C.POINTER(sph_grid), _f, _f,
+                                           C.POINTER(C.c_double)]),
+    "sph_rollout_backward": (C.c_int, [_vp, _f, _f, C.POINTER(C.c_double)]),
     "sph_make_configuration2": (C.c_int, [_f, _f, C.c_float, C.c_uint32, C.c_uint32, C.c_float,
                                           C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                           C.POINTER(sph_config2)]),

@@ -13,46 +13,21 @@
 
 using namespace sph;
 
-struct sph_solver {
-    sph_config cfg;
-    SimParams P;
-    cudaStream_t stream = nullptr;
-    uint32_t n = 0, nb = 0, ncells = 0;
-    int key_bits = 0;
-    float4* pos = nullptr;   // state, sorted order of the last step
-    float4* vel = nullptr;
-    float4* spos = nullptr;  // working copies in the current step's sorted order
-    float4* svel = nullptr;
-    float* rho = nullptr;
-    float2* aux = nullptr;
-    uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
-    uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
-    uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
-    uint32_t* keys[2] = {nullptr, nullptr};
-    uint32_t* vals[2] = {nullptr, nullptr};
-    uint2* cells = nullptr;
-    uint2* bcells = nullptr;
-    float4* bpos = nullptr;
-    float* stage = nullptr;  // device staging for packed readback
-    void* sort_mem = nullptr;
-    SortScratch sort;
-    uint32_t* err = nullptr;  // device error word
-    uint32_t* err_host = nullptr;
-    int force_timeout = 0;
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = 0.0f;
-};
+#include "single_scale_solver.h"
+
+using namespace sph_ss;
 
 namespace {
 
 int free_solver(sph_solver* s) {
     if (!s) return SPH_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    sph_rollout_release(s);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->err,     s->stage, s->nbr, s->nbr_count,
-                    s->bnear};
+                    s->bnear,   s->pos0};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->err_host) cudaFreeHost(s->err_host);
@@ -67,10 +42,12 @@ int dalloc(T** p, size_t count) {
     return SPH_OK;
 }
 
-inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
+}  // namespace
+
+namespace sph_ss {
 
 // hash -> onesweep sort -> reorder + cell ranges (Solver.cu:1098-1140).
-void enqueue_neighborhood(sph_solver* s) {
+int enqueue_neighborhood(sph_solver* s) {
     cudaStream_t st = s->stream;
     int passes = sort_passes(s->key_bits);
     cudaMemsetAsync(s->cells, 0xFF, sizeof(uint2) * s->ncells, st);
@@ -83,6 +60,7 @@ void enqueue_neighborhood(sph_solver* s) {
     gather_cells_kernel<true><<<blocks_for(s->n), 256, 0, st>>>(
         s->keys[out], s->vals[out], s->n, s->P.g, s->pos, s->vel, s->spos, s->svel, s->cells,
         s->err);
+    return out;
 }
 
 void enqueue_density(sph_solver* s) {
@@ -118,6 +96,10 @@ int check_device_error(sph_solver* s) {
     }
     return SPH_OK;
 }
+
+}  // namespace sph_ss
+
+namespace {
 
 // Copies xyz of a float4 device array into a host AoS array, in sorted order
 // or by the persistent ids in pos.w; the packing runs on the device so the
@@ -184,6 +166,7 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     TRY(dalloc(&s->cells, s->ncells));
     TRY(dalloc(&s->bcells, s->ncells));
     TRY(dalloc(&s->bpos, n_boundary));
+    TRY(dalloc(&s->pos0, n_fluid));
     TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
     s->sort = sort_scratch_from(s->sort_mem, nmax);
     TRY(dalloc(&s->err, 1));
@@ -209,6 +192,7 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
         if (n_fluid) {
             TRY(check_cuda(cudaMemcpyAsync(s->pos, hp.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
             TRY(check_cuda(cudaMemcpyAsync(s->vel, hv.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->pos0, hp.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
         }
         // Boundary: hashed and sorted once on the fluid grid (Solver.cu:1013-1055).
         TRY(check_cuda(cudaMemsetAsync(s->bcells, 0xFF, sizeof(uint2) * s->ncells, s->stream), "memset", __FILE__, __LINE__));

@@ -1,0 +1,56 @@
+// single_scale_solver.h -- the single-scale solver handle, shared by the step
+// (single_scale.cu) and the differentiable rollout (adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/sph2s.h"
+#include "common.cuh"
+#include "radix_sort.cuh"
+
+namespace sph {
+struct Rollout;  // tape of a differentiable rollout (adjoint.cu)
+}
+
+struct sph_solver {
+    sph_config cfg;
+    sph::SimParams P;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0, nb = 0, ncells = 0;
+    int key_bits = 0;
+    float4* pos = nullptr;   // state, sorted order of the last step
+    float4* vel = nullptr;
+    float4* spos = nullptr;  // working copies in the current step's sorted order
+    float4* svel = nullptr;
+    float* rho = nullptr;
+    float2* aux = nullptr;
+    uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
+    uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
+    uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* vals[2] = {nullptr, nullptr};
+    uint2* cells = nullptr;
+    uint2* bcells = nullptr;
+    float4* bpos = nullptr;
+    float4* pos0 = nullptr;  // positions at creation, creation order (rollout restarts)
+    float* stage = nullptr;  // device staging for packed readback
+    void* sort_mem = nullptr;
+    sph::SortScratch sort;
+    uint32_t* err = nullptr;  // device error word
+    uint32_t* err_host = nullptr;
+    int force_timeout = 0;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.0f;
+    sph::Rollout* rollout = nullptr;
+};
+
+namespace sph_ss {
+// hash -> onesweep sort -> reorder + cell ranges; returns the index of the
+// key/value buffers that hold the sorted keys and the permutation.
+int enqueue_neighborhood(sph_solver* s);
+void enqueue_density(sph_solver* s);
+void enqueue_force(sph_solver* s, float dt);
+int check_device_error(sph_solver* s);
+inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
+}  // namespace sph_ss
+
+// Releases the rollout tape (adjoint.cu).
+void sph_rollout_release(sph_solver* s);

@@ -125,3 +125,13 @@ def batched_scenes(num: int = 256, seed: int = 2, n_min: int = 4096, n_max: int 
                        bulk_modulus=BULK_MODULUS * float(k_scale[i]))
         out.append(sc)
     return out
+
+
+def differentiable_scene(lattice=(32, 64, 32), spacing: float = 1 / 64, seed: int = 0):
+    """The differentiable-rollout workload: a 32 x 64 x 32 lattice (64 along y)
+    at s = 1/64 (65,536 particles), h = 2s, dt = 1e-4; target initial
+    velocities N(0, 0.1^2) per component (seed 1)."""
+    sc = dam_break(spacing, lattice, seed=seed, dt=1e-4)
+    rng = np.random.default_rng(1)
+    v_target = rng.normal(0.0, 0.1, (sc.fluid.num_particles, 3)).astype(np.float32)
+    return sc, v_target

@@ -200,6 +200,30 @@ class Solver:
             uptr(r["nbr_fluid"]), uptr(r["nbr_boundary"]), fptr(r["rho"]), fptr(r["acc"])))
         return r
 
+    # ---- differentiable rollout ------------------------------------------
+    def rollout_forward(self, v0, viscosity: float, dt: float, steps: int,
+                        checkpoint_every: int = 20) -> None:
+        v = None if v0 is None else _as_xyz(v0, self.num_fluid, "v0")
+        check(lib().sph_rollout_forward(self._h, fptr(v), C.c_float(viscosity), C.c_float(dt),
+                                        int(steps), int(checkpoint_every)))
+
+    def rollout_density_loss(self, nodes: sph_grid, target=None):
+        """Splat field on the node grid, and the loss against `target` if given."""
+        nn = Grid.compute_num_grid_cells(nodes)
+        field = np.empty(nn, np.float32)
+        t = None if target is None else np.ascontiguousarray(target, np.float32).reshape(-1)
+        loss = C.c_double(0.0)
+        check(lib().sph_rollout_density_loss(self._h, C.byref(nodes), fptr(t), fptr(field),
+                                             C.byref(loss)))
+        return field, (loss.value if t is not None else None)
+
+    def rollout_backward(self):
+        gv = np.empty((self.num_fluid, 3), np.float32)
+        gx = np.empty((self.num_fluid, 3), np.float32)
+        gmu = C.c_double(0.0)
+        check(lib().sph_rollout_backward(self._h, fptr(gv), fptr(gx), C.byref(gmu)))
+        return gv, gx, gmu.value
+
     def profile_phases(self, dt: float, steps: int) -> dict:
         """Mean ms per step of (neighbourhood, density, force+integrate), CUDA events."""
         ms = np.zeros(3, np.float32)
