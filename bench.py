@@ -239,6 +239,45 @@ def measure_batched(steps: int, warmup: int = 3):
                       "each scene synchronised before the next starts"}
 
 
+def measure_adjoint(steps: int = 200, every: int = 20, reps: int = 3):
+    """65,536-particle differentiable rollout (T steps, checkpoints every K):
+    forward (with checkpoints) and backward (segment recompute + adjoint
+    kernels) wall time per rollout, synchronous calls, best of `reps`."""
+    import torch
+
+    from sph2s_final_gb300 import scenes
+    from sph2s_final_gb300.autograd import node_grid
+    from sph2s_final_gb300.solver import Solver
+
+    sc, vt = scenes.differentiable_scene()
+    with Solver(sc.fluid, sc.boundary, sc.config) as s:
+        s.rollout_forward(vt, 5.0, sc.dt, steps, every)
+        target, _ = s.rollout_density_loss(node_grid())
+        v0 = np.zeros_like(vt)
+        fw, bw, plain = [], [], []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.rollout_forward(v0, 5.0, sc.dt, steps, every)
+            t1 = time.perf_counter()
+            _, loss = s.rollout_density_loss(node_grid(), target)
+            t2 = time.perf_counter()
+            s.rollout_backward()
+            t3 = time.perf_counter()
+            fw.append(t1 - t0)
+            bw.append(t3 - t2)
+            s.sync()
+            t4 = time.perf_counter()
+            s.advance(sc.dt, steps)
+            s.sync()
+            plain.append(time.perf_counter() - t4)
+    f, b, p = min(fw), min(bw), min(plain)
+    return {"particles": sc.fluid.num_particles, "steps": steps, "checkpoint_every": every,
+            "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "plain_forward_ms": 1e3 * p,
+            "adjoint_over_forward": b / f, "adjoint_over_plain_forward": b / p,
+            "loss": loss, "timing": "host clock around synchronous calls, best of 3"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -379,6 +418,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds)
     if ws == 1 and not args.no_extras:
         line["batched"] = measure_batched(args.batched_steps)
+        line["adjoint"] = measure_adjoint()
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
