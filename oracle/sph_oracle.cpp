@@ -33,13 +33,17 @@
 // array position (a stable sort); this oracle does the same.  Cell tables are
 // indexed by the reference's linear hash.
 //
-// Parity unpinned against outputs of the reference itself: the reference ships
-// no tests, fixtures or golden vectors and cannot run on these machines (a
-// CUDA 5.0 / OpenGL program with no CPU path).  The restatement is checked
-// instead by known-answer cases derived by hand from the reference formulas
-// (tests/test_oracle.py).  The sort is a third-party dependency of the
-// reference (Thrust, bundled with CUDA 5.0, not vendored); its only contract
-// used here is "ascending by key", with ties in input order.
+// Parity pins: the reference ships no tests, fixtures or golden vectors and
+// cannot run as a program here (CUDA 5.0 / Windows / OpenGL, no CPU path), but
+// its single-scale device code compiles unmodified for sm_103a
+// (oracle/ref_build.py) and runs on the GPU under oracle/ref_harness.cu, which
+// replays its host sequence.  tests/golden/ref_*.npz hold those outputs and
+// tests/test_oracle_vs_reference.py checks this restatement against them
+// (hashes and sorted order bit-exact, fields to ~3e-7); tests/test_oracle.py
+// adds known-answer cases derived by hand from the reference formulas.  The
+// sort is a third-party dependency of the reference (Thrust, bundled with
+// CUDA 5.0, not vendored); its only contract used here is "ascending by key",
+// with ties in input order.
 // ============================================================================
 #include <cmath>
 #include <cstdint>

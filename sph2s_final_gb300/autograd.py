@@ -63,4 +63,4 @@ def fit_initial_state(solver: Solver, target, dt: float, steps: int, iters: int 
         loss.backward()
         opt.step()
         hist.append({"loss": float(loss.detach()), "mu": float(log_mu.detach().exp())})
-    return hist, v0.detach(), float(log_mu.exp())
+    return hist, v0.detach(), float(log_mu.detach().exp())
