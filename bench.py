@@ -291,7 +291,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     ro.advance(sc.dt, 1)
     one = time.perf_counter() - t0
-    budget = 120.0
+    budget = 90.0
     warm = min(args.warmup, max(0, int(0.2 * budget / one)))
     steps = max(1, min(args.steps, int(budget / one)))
     ro.advance(sc.dt, warm)
@@ -300,6 +300,7 @@ def run_reference(args):
     el = time.perf_counter() - t0
     ro.close()
     v = n * steps / el
+    ref_gpu = reference_kernels_on_gpu(sc, args)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
         "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
@@ -310,8 +311,29 @@ def run_reference(args):
                          "sample": f"FP64 CPU restatement of the reference step (the reference has "
                                    f"no CPU path), {steps} of {args.steps} requested steps"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": ref_gpu,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_kernels_on_gpu(sc, args):
+    """The reference's own step kernels (its Solver.cu compiled for sm_103a) and its
+    host sequence (thrust::sort_by_key per step), timed with CUDA events on this GPU."""
+    from oracle import ref_build
+    try:
+        if not ref_build.CUBIN.exists():
+            return {"unavailable": "reference kernels not built (oracle/_ref/ss_solver.cubin "
+                                   "is made where the reference checkout is present)"}
+        ms = ref_build.time_reference_kernels(sc.config, sc.fluid.positions,
+                                              sc.boundary.positions, args.steps, sc.dt,
+                                              args.warmup)
+    except Exception as e:  # reported, not fatal: the CPU port above is the arm's value
+        return {"unavailable": f"{type(e).__name__}: {str(e).splitlines()[0][:200]}"}
+    n = sc.fluid.num_particles
+    return {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.steps,
+            "warmup": max(1, args.warmup),
+            "kind": "reference kernels (Solver.cu, unmodified, sm_103a) + its thrust sort, "
+                    "CUDA events around whole steps"}
 
 
 def run_ours(args):

@@ -14,7 +14,12 @@
 // starts from rest) and a persistent id per particle, gathered through the
 // sort's permutation, so results can be matched particle by particle.
 //
-// usage: ref_harness <cubin> <input.bin> <output.bin>
+// usage: ref_harness <cubin> <input.bin> <output.bin> [--time W]
+//   --time W: run W untimed steps first, then time the input's steps with
+//             CUDA events around each whole step (the reference's own
+//             CUDA::Timer around Advance, Solver.cu:1084-1095) and print
+//             "ref_harness_ms_per_step <ms>"; the output file is still written,
+//             but the timed steps do not track persistent ids (W >= 1).
 //   input : "SPHREF01" | config (64 bytes, SolverConfiguration layout) |
 //           u32 n, u32 nb, u32 steps, f32 dt | f32 x[3n] | f32 v[3n] | f32 b[3nb]
 //   output: "SPHOUT01" | u32 n, u32 ncells |
@@ -111,8 +116,13 @@ std::vector<T> down(const T* d, size_t count) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc != 4) {
-        std::fprintf(stderr, "usage: ref_harness <cubin> <input.bin> <output.bin>\n");
+    if (argc != 4 && !(argc == 6 && std::strcmp(argv[4], "--time") == 0)) {
+        std::fprintf(stderr, "usage: ref_harness <cubin> <input.bin> <output.bin> [--time W]\n");
+        return 1;
+    }
+    const int warm = argc == 6 ? std::atoi(argv[5]) : -1;
+    if (argc == 6 && warm < 1) {
+        std::fprintf(stderr, "ref_harness: --time needs at least one warm-up step\n");
         return 1;
     }
     FILE* in = std::fopen(argv[2], "rb");
@@ -196,7 +206,15 @@ int main(int argc, char** argv) {
     wr(out, "SPHOUT01", 8);
     wr(out, &n, 1);
     wr(out, &nc, 1);
-    for (uint32_t s = 0; s < steps; ++s) {
+    cudaEvent_t ev0, ev1;
+    RT(cudaEventCreate(&ev0));
+    RT(cudaEventCreate(&ev1));
+    const uint32_t total = steps + (uint32_t)(warm > 0 ? warm : 0);
+    for (uint32_t s = 0; s < total; ++s) {
+        if (warm >= 0 && s == (uint32_t)warm) {
+            RT(cudaDeviceSynchronize());
+            RT(cudaEventRecord(ev0));
+        }
         // computeNeighborhoods (Solver.cu:1098-1140)
         void* h[] = {&hashs, &ids, &pos, &n};
         launch(fHash, n, h);
@@ -204,7 +222,8 @@ int main(int argc, char** argv) {
             thrust::sort_by_key(thrust::device_ptr<unsigned>(hashs),
                                 thrust::device_ptr<unsigned>(hashs + n),
                                 thrust::device_ptr<unsigned>(ids));
-        if (n) {
+        // Timed steps skip the harness-only id tracking (final ids then stale).
+        if (n && (warm < 0 || s < (uint32_t)warm)) {
             thrust::gather(thrust::device_ptr<unsigned>(ids), thrust::device_ptr<unsigned>(ids + n),
                            thrust::device_ptr<unsigned>(pid), thrust::device_ptr<unsigned>(pid2));
             std::swap(pid, pid2);
@@ -230,6 +249,13 @@ int main(int argc, char** argv) {
         }
         void* it[] = {&pos, &vel, &acc, &tpos, &tvel, &dt, &n};
         launch(fInt, n, it);
+    }
+    if (warm >= 0) {
+        RT(cudaEventRecord(ev1));
+        RT(cudaEventSynchronize(ev1));
+        float ms = 0.0f;
+        RT(cudaEventElapsedTime(&ms, ev0, ev1));
+        std::printf("ref_harness_ms_per_step %.6f\n", steps ? ms / (float)steps : 0.0f);
     }
     RT(cudaDeviceSynchronize());
     wr(out, down(pos, 3 * (size_t)n).data(), 3 * (size_t)n);
