@@ -33,6 +33,7 @@ extern "C" {
 #define SPH_E_CAPACITY 2 /* particle or cell count beyond what the ABI supports */
 #define SPH_E_CUDA 3     /* a CUDA runtime call failed (incl. allocation) */
 #define SPH_E_TIMEOUT 4  /* a bounded device-side wait gave up; results invalid */
+#define SPH_E_IO 5       /* a file could not be opened or written */
 
 /* Readback order. */
 #define SPH_ORDER_SORTED 0 /* array order of the last step (the reference's order) */
@@ -116,6 +117,31 @@ int sph_counts(sph_solver* s, uint32_t* n_fluid, uint32_t* n_boundary);
 /* Stream the handle enqueues on (a cudaStream_t). */
 void* sph_stream(sph_solver* s);
 int sph_destroy(sph_solver* s);
+
+/* ---- headless state I/O ---------------------------------------------------
+ * Replaces the reference's only output path, the GL vertex buffer mapped by
+ * ParticleData::Map/Unmap (SPH2S_FINAL_SINGLE_SCALE/ParticleData.cpp:47-66)
+ * and the rendered frames of VideoWriter::CaptureFrame
+ * (SPH2S_FINAL_SINGLE_SCALE/VideoWriter/VideoWriter.cpp:41-49). */
+
+/* Field mask of frame records. */
+#define SPH_FIELD_POSITIONS 1u
+#define SPH_FIELD_VELOCITIES 2u
+#define SPH_FIELD_DENSITIES 4u /* single scale only */
+#define SPH_FIELD_BLEND 8u     /* two scale only: blend coefficient and state bits */
+
+/* Steps advanced since creation (a state carries it across save / resume). */
+int sph_step_count(sph_solver* s, uint64_t* steps);
+/* Serialises the complete solver state into dst (host memory).  With dst ==
+ * NULL only *bytes (the size needed) is written.  A solver created from the
+ * state continues bit for bit like this one.  Waits for queued steps. */
+int sph_save_state(sph_solver* s, void* dst, uint64_t capacity, uint64_t* bytes);
+/* Creates a solver from a buffer written by sph_save_state; SPH_E_INVALID if
+ * the buffer is not a single-scale state or fails its checksum. */
+int sph_create_from_state(const void* src, uint64_t bytes, sph_solver** out);
+/* Appends (append != 0) or writes one frame record to path: the current step
+ * number and the requested fields, in input (persistent id) order. */
+int sph_write_frame(sph_solver* s, const char* path, uint32_t fields, int32_t append);
 
 /* Parity instrumentation for the current state, without advancing it:
  * hashes, sorts and reorders exactly as the next step will, and returns, each
@@ -233,6 +259,15 @@ int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sor
                            float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
                            uint32_t* nbr_boundary);
 int sph2_destroy(sph_solver2* s);
+/* Two-scale state I/O, as sph_save_state / sph_create_from_state: both
+ * populations with blend coefficients, state bits and group ids, the group
+ * and id counters, capacities and the presorted boundary. */
+int sph2_step_count(sph_solver2* s, uint64_t* steps);
+int sph2_save_state(sph_solver2* s, void* dst, uint64_t capacity, uint64_t* bytes);
+int sph2_create_from_state(const void* src, uint64_t bytes, sph_solver2** out);
+/* Frame record of both populations in their current order, each preceded by
+ * its persistent ids; fields: positions, velocities, blend. */
+int sph2_write_frame(sph_solver2* s, const char* path, uint32_t fields, int32_t append);
 
 /* ---- batched single-scale scenes --------------------------------------- */
 

@@ -15,10 +15,12 @@ SPH_E_INVALID = 1
 SPH_E_CAPACITY = 2
 SPH_E_CUDA = 3
 SPH_E_TIMEOUT = 4
+SPH_E_IO = 5
 SPH_ORDER_SORTED = 0
 SPH_ORDER_BY_ID = 1
 
-_STATUS = {1: "SPH_E_INVALID", 2: "SPH_E_CAPACITY", 3: "SPH_E_CUDA", 4: "SPH_E_TIMEOUT"}
+_STATUS = {1: "SPH_E_INVALID", 2: "SPH_E_CAPACITY", 3: "SPH_E_CUDA", 4: "SPH_E_TIMEOUT",
+           5: "SPH_E_IO"}
 
 
 class SphError(RuntimeError):
@@ -133,6 +135,14 @@ SIGNATURES = {
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_uint32, C.c_int32, C.c_void_p]),
+    "sph_step_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    "sph_save_state": (C.c_int, [_vp, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "sph_create_from_state": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(_vp)]),
+    "sph_write_frame": (C.c_int, [_vp, C.c_char_p, C.c_uint32, C.c_int32]),
+    "sph2_step_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    "sph2_save_state": (C.c_int, [_vp, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "sph2_create_from_state": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(_vp)]),
+    "sph2_write_frame": (C.c_int, [_vp, C.c_char_p, C.c_uint32, C.c_int32]),
     "sph_last_error": (C.c_char_p, []),
 }
 

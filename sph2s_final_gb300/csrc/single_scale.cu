@@ -97,37 +97,10 @@ int check_device_error(sph_solver* s) {
     return SPH_OK;
 }
 
-}  // namespace sph_ss
-
-namespace {
-
-// Copies xyz of a float4 device array into a host AoS array, in sorted order
-// or by the persistent ids in pos.w; the packing runs on the device so the
-// host only receives 12 bytes per particle.
-int download_xyz(sph_solver* s, const float4* dsrc, float* dst, int32_t order) {
-    if (s->n == 0) return SPH_OK;
-    if (!s->stage) SPH_CUDA(cudaMalloc(&s->stage, 12 * (size_t)s->n));
-    pack_xyz_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(dsrc, s->pos, s->n,
-                                                             order == SPH_ORDER_BY_ID, s->stage);
-    SPH_CUDA(cudaGetLastError());
-    SPH_CUDA(cudaMemcpyAsync(dst, s->stage, 12 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
-    SPH_CUDA(cudaStreamSynchronize(s->stream));
-    return SPH_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_fluid,
-               const float* boundary_xyz, uint32_t n_boundary, const float* velocity_xyz,
-               sph_solver** out) {
-    if (!config || !out) return fail(SPH_E_INVALID, "sph_create: NULL config or output handle");
+int create_solver(const sph_config* config, const float4* hpos, const float4* hvel,
+                  const float4* hpos0, uint32_t n_fluid, const float4* hbound, uint32_t n_boundary,
+                  uint64_t step, sph_solver** out) {
     *out = nullptr;
-    if (n_fluid && !fluid_xyz) return fail(SPH_E_INVALID, "sph_create: NULL fluid positions");
-    if (n_boundary && !boundary_xyz) return fail(SPH_E_INVALID, "sph_create: NULL boundary positions");
-    if (n_fluid > kMaxParticles || n_boundary > kMaxParticles)
-        return fail(SPH_E_CAPACITY, "sph_create: more than 2^30 particles");
     SimParams P;
     int rc = make_sim_params(*config, &P);
     if (rc != SPH_OK) return rc;
@@ -139,6 +112,7 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     s->nb = n_boundary;
     s->ncells = sph_grid_num_cells(&config->grid);
     s->key_bits = 3 * P.g.mbits;
+    s->step = step;
 #define TRY(x)                      \
     do {                            \
         int _r = (x);               \
@@ -178,34 +152,19 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     }
     TRY(check_cuda(cudaMemsetAsync(s->rho, 0, 4 * (size_t)(n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
 
-    // Upload the fluid state as float4 with the persistent id in w.
+    // Upload the fluid state (float4, persistent id in w).
     {
-        std::vector<float4> hp(n_fluid), hv(n_fluid);
-        for (uint32_t i = 0; i < n_fluid; ++i) {
-            float w;
-            std::memcpy(&w, &i, 4);
-            hp[i] = make_float4(fluid_xyz[3 * i], fluid_xyz[3 * i + 1], fluid_xyz[3 * i + 2], w);
-            hv[i] = velocity_xyz ? make_float4(velocity_xyz[3 * i], velocity_xyz[3 * i + 1],
-                                               velocity_xyz[3 * i + 2], 0.0f)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
         if (n_fluid) {
-            TRY(check_cuda(cudaMemcpyAsync(s->pos, hp.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
-            TRY(check_cuda(cudaMemcpyAsync(s->vel, hv.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
-            TRY(check_cuda(cudaMemcpyAsync(s->pos0, hp.data(), sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->pos, hpos, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->vel, hvel, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->pos0, hpos0, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
         }
         // Boundary: hashed and sorted once on the fluid grid (Solver.cu:1013-1055).
         TRY(check_cuda(cudaMemsetAsync(s->bcells, 0xFF, sizeof(uint2) * s->ncells, s->stream), "memset", __FILE__, __LINE__));
         if (n_boundary) {
-            std::vector<float4> hb(n_boundary);
-            for (uint32_t i = 0; i < n_boundary; ++i) {
-                float w;
-                std::memcpy(&w, &i, 4);
-                hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
-            }
             float4* braw = nullptr;
             TRY(dalloc(&braw, n_boundary));
-            cudaError_t e = cudaMemcpyAsync(braw, hb.data(), sizeof(float4) * n_boundary, cudaMemcpyHostToDevice, s->stream);
+            cudaError_t e = cudaMemcpyAsync(braw, hbound, sizeof(float4) * n_boundary, cudaMemcpyHostToDevice, s->stream);
             if (e == cudaSuccess) {
                 int passes = sort_passes(s->key_bits);
                 sort_reset(s->sort, s->stream);
@@ -234,6 +193,56 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     return SPH_OK;
 }
 
+}  // namespace sph_ss
+
+namespace {
+
+// Copies xyz of a float4 device array into a host AoS array, in sorted order
+// or by the persistent ids in pos.w; the packing runs on the device so the
+// host only receives 12 bytes per particle.
+int download_xyz(sph_solver* s, const float4* dsrc, float* dst, int32_t order) {
+    if (s->n == 0) return SPH_OK;
+    if (!s->stage) SPH_CUDA(cudaMalloc(&s->stage, 12 * (size_t)s->n));
+    pack_xyz_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(dsrc, s->pos, s->n,
+                                                             order == SPH_ORDER_BY_ID, s->stage);
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaMemcpyAsync(dst, s->stage, 12 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_fluid,
+               const float* boundary_xyz, uint32_t n_boundary, const float* velocity_xyz,
+               sph_solver** out) {
+    if (!config || !out) return fail(SPH_E_INVALID, "sph_create: NULL config or output handle");
+    *out = nullptr;
+    if (n_fluid && !fluid_xyz) return fail(SPH_E_INVALID, "sph_create: NULL fluid positions");
+    if (n_boundary && !boundary_xyz) return fail(SPH_E_INVALID, "sph_create: NULL boundary positions");
+    if (n_fluid > kMaxParticles || n_boundary > kMaxParticles)
+        return fail(SPH_E_CAPACITY, "sph_create: more than 2^30 particles");
+    // float4 with the persistent id (fluid) / input index (boundary) in w
+    std::vector<float4> hp(n_fluid), hv(n_fluid), hb(n_boundary);
+    for (uint32_t i = 0; i < n_fluid; ++i) {
+        float w;
+        std::memcpy(&w, &i, 4);
+        hp[i] = make_float4(fluid_xyz[3 * i], fluid_xyz[3 * i + 1], fluid_xyz[3 * i + 2], w);
+        hv[i] = velocity_xyz ? make_float4(velocity_xyz[3 * i], velocity_xyz[3 * i + 1],
+                                           velocity_xyz[3 * i + 2], 0.0f)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (uint32_t i = 0; i < n_boundary; ++i) {
+        float w;
+        std::memcpy(&w, &i, 4);
+        hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
+    }
+    return sph_ss::create_solver(config, hp.data(), hv.data(), hp.data(), n_fluid, hb.data(),
+                                 n_boundary, 0, out);
+}
+
 int sph_advance(sph_solver* s, float dt, int32_t steps) {
     if (!s) return fail(SPH_E_INVALID, "sph_advance: NULL handle");
     if (steps < 0 || !std::isfinite(dt)) return fail(SPH_E_INVALID, "sph_advance: bad dt or steps");
@@ -241,6 +250,7 @@ int sph_advance(sph_solver* s, float dt, int32_t steps) {
     if (s->force_timeout) {
         for (int k = 0; k < steps; ++k) enqueue_step(s, dt);
         SPH_CUDA(cudaGetLastError());
+        s->step += (uint64_t)steps;
         return SPH_OK;
     }
     if (!s->graph || s->graph_dt != dt) {
@@ -261,6 +271,7 @@ int sph_advance(sph_solver* s, float dt, int32_t steps) {
         s->graph_dt = dt;
     }
     for (int k = 0; k < steps; ++k) SPH_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    s->step += (uint64_t)steps;
     return SPH_OK;
 }
 

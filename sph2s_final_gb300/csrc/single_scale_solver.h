@@ -39,6 +39,7 @@ struct sph_solver {
     int force_timeout = 0;
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.0f;
+    uint64_t step = 0;  // steps advanced since creation (carried by saved states)
     sph::Rollout* rollout = nullptr;
 };
 
@@ -49,6 +50,12 @@ int enqueue_neighborhood(sph_solver* s);
 void enqueue_density(sph_solver* s);
 void enqueue_force(sph_solver* s, float dt);
 int check_device_error(sph_solver* s);
+// Creates a handle from host float4 arrays: fluid positions (persistent id in
+// w) and velocities in the order the next step starts from, creation-time
+// positions (rollout restarts), boundary positions (presorted here).
+int create_solver(const sph_config* config, const float4* hpos, const float4* hvel,
+                  const float4* hpos0, uint32_t n_fluid, const float4* hbound, uint32_t n_boundary,
+                  uint64_t step, sph_solver** out);
 inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
 }  // namespace sph_ss
 

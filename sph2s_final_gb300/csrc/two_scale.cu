@@ -8,9 +8,12 @@
 // deterministic.  The host reads the new population sizes back after each
 // step, as the reference does (Solver.cu:1633-1638).
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 #include "errors.h"
+#include "state_format.h"
 #include "host_params.h"
 #include "radix_sort.cuh"
 #include "scan.cuh"
@@ -75,6 +78,7 @@ struct sph_solver2 {
     uint32_t group_base = 0;
     uint32_t stats[6] = {0, 0, 0, 0, 0, 0};
     uint32_t next_id[2] = {0, 0};  // persistent id of the next particle created (LOW, HIGH)
+    uint64_t step = 0;             // steps advanced since creation
     std::vector<void*> owned;
 };
 
@@ -306,25 +310,142 @@ int ts_step(sph_solver2* s, float dt) {
     return check_err2(s);
 }
 
-int upload_pop(sph_solver2* s, int r, const float* xyz, uint32_t n) {
-    Pop& p = s->pop[r];
-    std::vector<float4> hp(n), hv(n);
-    std::vector<int32_t> hs(n, r == 1 ? 4 : 0);  // HIGH states start at 4 (Solver.cu:1537-1543)
-    std::vector<uint32_t> hg(n, kNoGroup);
+// Host copy of one population's persistent state, in the order the next
+// step starts from: position (persistent id in w), velocity (blend
+// coefficient lambda in w), state bits, group id.
+struct HostPop {
+    std::vector<float4> pos, vel;
+    std::vector<int32_t> stt;
+    std::vector<uint32_t> grp;
+};
+
+HostPop initial_pop(int r, const float* xyz, uint32_t n) {
+    HostPop h;
+    h.pos.resize(n);
+    h.vel.assign(n, make_float4(0.f, 0.f, 0.f, 1.0f));  // lambda starts at 1 (Solver.cu:1371)
+    h.stt.assign(n, r == 1 ? 4 : 0);  // HIGH states start at 4 (Solver.cu:1537-1543)
+    h.grp.assign(n, kNoGroup);
     for (uint32_t i = 0; i < n; ++i) {
         float w;
         std::memcpy(&w, &i, 4);
-        hp[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], w);
-        hv[i] = make_float4(0.f, 0.f, 0.f, 1.0f);  // lambda starts at 1 (Solver.cu:1371)
+        h.pos[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], w);
     }
+    return h;
+}
+
+int upload_pop(sph_solver2* s, int r, const HostPop& h) {
+    Pop& p = s->pop[r];
+    const uint32_t n = (uint32_t)h.pos.size();
     if (n) {
-        SPH_CUDA(cudaMemcpy(p.pos, hp.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
-        SPH_CUDA(cudaMemcpy(p.vel, hv.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
-        SPH_CUDA(cudaMemcpy(p.stt, hs.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
-        SPH_CUDA(cudaMemcpy(p.grp, hg.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.pos, h.pos.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.vel, h.vel.data(), 16 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.stt, h.stt.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(p.grp, h.grp.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
     }
     p.n = n;
     return SPH_OK;
+}
+
+// Allocates a handle for capacities capL / capH, uploads both populations,
+// sets the group and id counters and presorts the boundary (float4, input
+// index in w) on the LOW grid.
+int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, uint64_t capH,
+                   const HostPop* pops, const float4* hb, uint32_t n_boundary,
+                   uint32_t group_base, const uint32_t next_id[2], uint64_t step,
+                   sph_solver2** out) {
+    sph_solver2* s = new sph_solver2();
+    s->cfg = *config;
+    s->P = P;
+    s->nb = n_boundary;
+    s->next_id[0] = next_id[0];
+    s->next_id[1] = next_id[1];
+    s->group_base = group_base;
+    s->step = step;
+    s->cap_groups = (uint32_t)(capH / 8 * 4 + 64);
+#define TRY(x)                                 \
+    do {                                       \
+        int _r = (x);                          \
+        if (_r != SPH_OK) {                    \
+            std::string m = sph_last_error();  \
+            free_solver2(s);                   \
+            return fail(_r, m);                \
+        }                                      \
+    } while (0)
+    if (group_base > s->cap_groups) {
+        free_solver2(s);
+        return fail(SPH_E_INVALID, "two-scale state: group counter beyond the group capacity");
+    }
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], s->owned));
+    TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], s->owned));
+    const uint32_t nmax = (uint32_t)std::max<uint64_t>(std::max(capL, capH), n_boundary);
+    for (int b = 0; b < 2; ++b) {
+        TRY(dalloc(&s->keys[b], nmax, s->owned));
+        TRY(dalloc(&s->vals[b], nmax, s->owned));
+    }
+    TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
+    s->owned.push_back(s->sort_mem);
+    s->sort = sort_scratch_from(s->sort_mem, nmax);
+    TRY(dalloc(&s->scan_scratch, scan_scratch_words(std::max<uint32_t>(nmax, s->cap_groups)), s->owned));
+    TRY(dalloc(&s->tot, 4, s->owned));
+    TRY(dalloc(&s->gsum, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gready, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gmerge, s->cap_groups, s->owned));
+    TRY(dalloc(&s->moff, s->cap_groups, s->owned));
+    TRY(dalloc(&s->gacc, 6 * (size_t)s->cap_groups, s->owned));
+    TRY(dalloc(&s->ctl, kCtlWords, s->owned));
+    TRY(dalloc(&s->err, 1, s->owned));
+    TRY(dalloc(&s->bpos, n_boundary, s->owned));
+    TRY(dalloc(&s->bcells, s->pop[0].ncells, s->owned));
+    TRY(check_cuda(cudaMallocHost((void**)&s->ctl_host, 4 * kCtlWords), "pinned", __FILE__, __LINE__));
+    TRY(check_cuda(cudaMemset(s->err, 0, 4), "memset", __FILE__, __LINE__));
+    {
+        uint32_t c0[kCtlWords] = {0};
+        c0[kCtlPidH] = next_id[1];
+        c0[kCtlPidL] = next_id[0];
+        c0[kCtlGroupBase] = group_base;
+        TRY(check_cuda(cudaMemcpy(s->ctl, c0, sizeof(c0), cudaMemcpyHostToDevice), "ctl", __FILE__, __LINE__));
+    }
+    for (int b = 0; b < 2; ++b) {
+        TRY(check_cuda(cudaMemset(s->keys[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
+        TRY(check_cuda(cudaMemset(s->vals[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
+    }
+    TRY(upload_pop(s, 0, pops[0]));
+    TRY(upload_pop(s, 1, pops[1]));
+    // boundary: sorted once on the LOW grid (SPH2S_FINAL_TWO_SCALE/Solver.cu:1469-1527)
+    TRY(check_cuda(cudaMemset(s->bcells, 0xFF, sizeof(uint2) * s->pop[0].ncells), "memset", __FILE__, __LINE__));
+    if (n_boundary) {
+        float4* braw = nullptr;
+        cudaError_t e = cudaMalloc(&braw, 16 * (size_t)n_boundary);
+        if (e == cudaSuccess) e = cudaMemcpy(braw, hb, 16 * (size_t)n_boundary, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            const int passes = sort_passes(s->pop[0].key_bits);
+            sort_reset(s->sort, s->stream);
+            uint32_t hbk = blocks_for(n_boundary);
+            if (hbk > 1216) hbk = 1216;
+            hash_hist_kernel<<<hbk, 256, 0, s->stream>>>(braw, n_boundary, s->P.g[0], passes,
+                                                         s->keys[0], s->sort.hist);
+            sort_scan(passes, s->sort, s->stream);
+            const int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort,
+                                          s->err, 0, s->stream);
+            gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
+                s->keys[o], s->vals[o], n_boundary, s->P.g[0], braw, nullptr, s->bpos, nullptr,
+                s->bcells, s->err);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        }
+        if (braw) cudaFree(braw);
+        TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
+    }
+    TRY(check_err2(s));
+#undef TRY
+    *out = s;
+    return SPH_OK;
+}
+
+uint64_t ts_state_bytes(uint64_t n_low, uint64_t n_high, uint64_t nb) {
+    return sizeof(sph_io::StatePrefix) + sizeof(sph_config2) + 24 + 16 +
+           40 * (n_low + n_high) + 16 * nb + 8;
 }
 
 }  // namespace
@@ -381,93 +502,15 @@ int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
     if (capL < n_low || capH < n_high) return fail(SPH_E_CAPACITY, "sph2_create: capacity below the initial count");
     if (capL > kMaxParticles || capH > kMaxParticles || n_boundary > kMaxParticles)
         return fail(SPH_E_CAPACITY, "sph2_create: more than 2^30 particles");
-    sph_solver2* s = new sph_solver2();
-    s->cfg = *config;
-    s->P = P;
-    s->nb = n_boundary;
-    s->next_id[0] = n_low;
-    s->next_id[1] = n_high;
-    s->cap_groups = (uint32_t)(capH / 8 * 4 + 64);
-#define TRY(x)                                 \
-    do {                                       \
-        int _r = (x);                          \
-        if (_r != SPH_OK) {                    \
-            std::string m = sph_last_error();  \
-            free_solver2(s);                   \
-            return fail(_r, m);                \
-        }                                      \
-    } while (0)
-    TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
-    TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], s->owned));
-    TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], s->owned));
-    const uint32_t nmax = (uint32_t)std::max<uint64_t>(std::max(capL, capH), n_boundary);
-    for (int b = 0; b < 2; ++b) {
-        TRY(dalloc(&s->keys[b], nmax, s->owned));
-        TRY(dalloc(&s->vals[b], nmax, s->owned));
+    HostPop pops[2] = {initial_pop(0, low_xyz, n_low), initial_pop(1, high_xyz, n_high)};
+    std::vector<float4> hb(n_boundary);
+    for (uint32_t i = 0; i < n_boundary; ++i) {
+        float w;
+        std::memcpy(&w, &i, 4);
+        hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
     }
-    TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
-    s->owned.push_back(s->sort_mem);
-    s->sort = sort_scratch_from(s->sort_mem, nmax);
-    TRY(dalloc(&s->scan_scratch, scan_scratch_words(std::max<uint32_t>(nmax, s->cap_groups)), s->owned));
-    TRY(dalloc(&s->tot, 4, s->owned));
-    TRY(dalloc(&s->gsum, s->cap_groups, s->owned));
-    TRY(dalloc(&s->gready, s->cap_groups, s->owned));
-    TRY(dalloc(&s->gmerge, s->cap_groups, s->owned));
-    TRY(dalloc(&s->moff, s->cap_groups, s->owned));
-    TRY(dalloc(&s->gacc, 6 * (size_t)s->cap_groups, s->owned));
-    TRY(dalloc(&s->ctl, kCtlWords, s->owned));
-    TRY(dalloc(&s->err, 1, s->owned));
-    TRY(dalloc(&s->bpos, n_boundary, s->owned));
-    TRY(dalloc(&s->bcells, s->pop[0].ncells, s->owned));
-    TRY(check_cuda(cudaMallocHost((void**)&s->ctl_host, 4 * kCtlWords), "pinned", __FILE__, __LINE__));
-    TRY(check_cuda(cudaMemset(s->err, 0, 4), "memset", __FILE__, __LINE__));
-    {
-        uint32_t c0[kCtlWords] = {0};
-        c0[kCtlPidH] = n_high;
-        c0[kCtlPidL] = n_low;
-        TRY(check_cuda(cudaMemcpy(s->ctl, c0, sizeof(c0), cudaMemcpyHostToDevice), "ctl", __FILE__, __LINE__));
-    }
-    for (int b = 0; b < 2; ++b) {
-        TRY(check_cuda(cudaMemset(s->keys[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
-        TRY(check_cuda(cudaMemset(s->vals[b], 0, 4 * (size_t)nmax), "memset", __FILE__, __LINE__));
-    }
-    TRY(upload_pop(s, 0, low_xyz, n_low));
-    TRY(upload_pop(s, 1, high_xyz, n_high));
-    // boundary: sorted once on the LOW grid (SPH2S_FINAL_TWO_SCALE/Solver.cu:1469-1527)
-    TRY(check_cuda(cudaMemset(s->bcells, 0xFF, sizeof(uint2) * s->pop[0].ncells), "memset", __FILE__, __LINE__));
-    if (n_boundary) {
-        std::vector<float4> hb(n_boundary);
-        for (uint32_t i = 0; i < n_boundary; ++i) {
-            float w;
-            std::memcpy(&w, &i, 4);
-            hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
-        }
-        float4* braw = nullptr;
-        cudaError_t e = cudaMalloc(&braw, 16 * (size_t)n_boundary);
-        if (e == cudaSuccess) e = cudaMemcpy(braw, hb.data(), 16 * (size_t)n_boundary, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) {
-            const int passes = sort_passes(s->pop[0].key_bits);
-            sort_reset(s->sort, s->stream);
-            uint32_t hbk = blocks_for(n_boundary);
-            if (hbk > 1216) hbk = 1216;
-            hash_hist_kernel<<<hbk, 256, 0, s->stream>>>(braw, n_boundary, s->P.g[0], passes,
-                                                         s->keys[0], s->sort.hist);
-            sort_scan(passes, s->sort, s->stream);
-            const int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort,
-                                          s->err, 0, s->stream);
-            gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
-                s->keys[o], s->vals[o], n_boundary, s->P.g[0], braw, nullptr, s->bpos, nullptr,
-                s->bcells, s->err);
-            e = cudaGetLastError();
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        }
-        if (braw) cudaFree(braw);
-        TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
-    }
-    TRY(check_err2(s));
-#undef TRY
-    *out = s;
-    return SPH_OK;
+    const uint32_t next_id[2] = {n_low, n_high};
+    return create_solver2(config, P, capL, capH, pops, hb.data(), n_boundary, 0, next_id, 0, out);
 }
 
 int sph2_advance(sph_solver2* s, float dt, int32_t steps) {
@@ -477,6 +520,7 @@ int sph2_advance(sph_solver2* s, float dt, int32_t steps) {
     for (int k = 0; k < steps; ++k) {
         int rc = ts_step(s, dt);
         if (rc != SPH_OK) return rc;
+        ++s->step;
     }
     return SPH_OK;
 }
@@ -572,5 +616,156 @@ int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sor
 }
 
 int sph2_destroy(sph_solver2* s) { return free_solver2(s); }
+
+// ---- state I/O (formats in state_format.h) ---------------------------------
+// Two-scale state body:
+//   sph_config2 | u32 n_low, n_high, nb, group_base, next_low, next_high |
+//   u64 cap_low, cap_high |
+//   per population (LOW, HIGH): float4 pos[n] (id in w), float4 vel[n]
+//   (lambda in w), i32 state[n], u32 group[n] | float4 bpos[nb]
+
+int sph2_step_count(sph_solver2* s, uint64_t* steps) {
+    if (!s || !steps) return fail(SPH_E_INVALID, "sph2_step_count: NULL argument");
+    *steps = s->step;
+    return SPH_OK;
+}
+
+int sph2_save_state(sph_solver2* s, void* dst, uint64_t capacity, uint64_t* bytes) {
+    if (!s || !bytes) return fail(SPH_E_INVALID, "sph2_save_state: NULL handle or size output");
+    const uint64_t nL = s->pop[0].n, nH = s->pop[1].n;
+    const uint64_t need = ts_state_bytes(nL, nH, s->nb);
+    *bytes = need;
+    if (!dst) return SPH_OK;
+    if (capacity < need) return fail(SPH_E_CAPACITY, "sph2_save_state: buffer smaller than the state");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    int rc = check_err2(s);
+    if (rc != SPH_OK) return rc;
+    sph_io::Writer w{static_cast<unsigned char*>(dst)};
+    sph_io::StatePrefix pre;
+    std::memcpy(pre.magic, sph_io::kStateMagic, 8);
+    pre.version = sph_io::kStateVersion;
+    pre.kind = sph_io::kKindTwoScale;
+    pre.step = s->step;
+    w.put(&pre, sizeof(pre));
+    w.put(&s->cfg, sizeof(sph_config2));
+    const uint32_t counts[6] = {s->pop[0].n, s->pop[1].n, s->nb, s->group_base, s->next_id[0],
+                                s->next_id[1]};
+    w.put(counts, sizeof(counts));
+    const uint64_t caps[2] = {s->pop[0].cap, s->pop[1].cap};
+    w.put(caps, sizeof(caps));
+    for (int r = 0; r < 2; ++r) {
+        const Pop& p = s->pop[r];
+        const size_t n = p.n;
+        if (!n) continue;
+        SPH_CUDA(cudaMemcpy(w.take(16 * n), p.pos, 16 * n, cudaMemcpyDeviceToHost));
+        SPH_CUDA(cudaMemcpy(w.take(16 * n), p.vel, 16 * n, cudaMemcpyDeviceToHost));
+        SPH_CUDA(cudaMemcpy(w.take(4 * n), p.stt, 4 * n, cudaMemcpyDeviceToHost));
+        SPH_CUDA(cudaMemcpy(w.take(4 * n), p.grp, 4 * n, cudaMemcpyDeviceToHost));
+    }
+    if (s->nb) SPH_CUDA(cudaMemcpy(w.take(16 * (size_t)s->nb), s->bpos, 16 * (size_t)s->nb, cudaMemcpyDeviceToHost));
+    const uint64_t sum = sph_io::checksum(dst, w.off);
+    w.put(&sum, 8);
+    return SPH_OK;
+}
+
+int sph2_create_from_state(const void* src, uint64_t bytes, sph_solver2** out) {
+    if (!src || !out) return fail(SPH_E_INVALID, "sph2_create_from_state: NULL argument");
+    *out = nullptr;
+    sph_io::StatePrefix pre;
+    if (!sph_io::check_state(src, (size_t)bytes, sph_io::kKindTwoScale, &pre))
+        return fail(SPH_E_INVALID, "sph2_create_from_state: not a two-scale state, or corrupt");
+    sph_io::Reader r{static_cast<const unsigned char*>(src), (size_t)bytes - 8, sizeof(pre)};
+    sph_config2 cfg;
+    uint32_t c[6];
+    uint64_t caps[2];
+    if (!r.get(&cfg, sizeof(cfg)) || !r.get(c, sizeof(c)) || !r.get(caps, sizeof(caps)))
+        return fail(SPH_E_INVALID, "sph2_create_from_state: truncated header");
+    const uint32_t nb = c[2], group_base = c[3];
+    const uint32_t next_id[2] = {c[4], c[5]};
+    if (caps[0] > kMaxParticles || caps[1] > kMaxParticles || nb > kMaxParticles ||
+        c[0] > caps[0] || c[1] > caps[1])
+        return fail(SPH_E_CAPACITY, "sph2_create_from_state: counts beyond capacities or 2^30");
+    if (bytes != ts_state_bytes(c[0], c[1], nb))
+        return fail(SPH_E_INVALID, "sph2_create_from_state: size does not match the particle counts");
+    TSParams P;
+    int rc = make_ts_params(cfg, &P);
+    if (rc != SPH_OK) return rc;
+    HostPop pops[2];
+    for (int q = 0; q < 2; ++q) {
+        const uint32_t n = c[q];
+        HostPop& h = pops[q];
+        h.pos.resize(n);
+        h.vel.resize(n);
+        h.stt.resize(n);
+        h.grp.resize(n);
+        r.get(h.pos.data(), 16 * (size_t)n);
+        r.get(h.vel.data(), 16 * (size_t)n);
+        r.get(h.stt.data(), 4 * (size_t)n);
+        r.get(h.grp.data(), 4 * (size_t)n);
+        std::vector<unsigned char> seen(next_id[q], 0);
+        for (uint32_t i = 0; i < n; ++i) {
+            uint32_t id;
+            std::memcpy(&id, &h.pos[i].w, 4);
+            if (id >= next_id[q] || seen[id] || h.stt[i] < 0 || h.stt[i] > 15 ||
+                (h.grp[i] != kNoGroup && h.grp[i] >= group_base))
+                return fail(SPH_E_INVALID, "sph2_create_from_state: inconsistent ids, states or groups");
+            seen[id] = 1;
+        }
+    }
+    std::vector<float4> hb(nb);
+    r.get(hb.data(), 16 * (size_t)nb);
+    return create_solver2(&cfg, P, caps[0], caps[1], pops, hb.data(), nb, group_base, next_id,
+                          pre.step, out);
+}
+
+int sph2_write_frame(sph_solver2* s, const char* path, uint32_t fields, int32_t append) {
+    if (!s || !path) return fail(SPH_E_INVALID, "sph2_write_frame: NULL argument");
+    const uint32_t known = SPH_FIELD_POSITIONS | SPH_FIELD_VELOCITIES | SPH_FIELD_BLEND;
+    if (fields == 0 || (fields & ~known))
+        return fail(SPH_E_INVALID, "sph2_write_frame: fields must be a non-empty mask of "
+                                   "positions, velocities, blend");
+    struct Arrays {
+        std::vector<uint32_t> ids;
+        std::vector<float> x, v, lambda;
+        std::vector<int32_t> state;
+    } a[2];
+    for (int q = 0; q < 2; ++q) {
+        const size_t n = s->pop[q].n;
+        a[q].ids.resize(n);
+        if (fields & SPH_FIELD_POSITIONS) a[q].x.resize(3 * n);
+        if (fields & SPH_FIELD_VELOCITIES) a[q].v.resize(3 * n);
+        if (fields & SPH_FIELD_BLEND) {
+            a[q].lambda.resize(n);
+            a[q].state.resize(n);
+        }
+        int rc = sph2_get_state(s, q, a[q].x.empty() ? nullptr : a[q].x.data(),
+                                a[q].v.empty() ? nullptr : a[q].v.data(),
+                                a[q].lambda.empty() ? nullptr : a[q].lambda.data(),
+                                a[q].state.empty() ? nullptr : a[q].state.data(), nullptr,
+                                a[q].ids.data());
+        if (rc != SPH_OK) return rc;
+    }
+    FILE* f = std::fopen(path, append ? "ab" : "wb");
+    if (!f) return fail(SPH_E_IO, std::string("sph2_write_frame: cannot open ") + path);
+    sph_io::FramePrefix pre;
+    std::memcpy(pre.magic, sph_io::kFrameMagic, 8);
+    pre.kind = sph_io::kKindTwoScale;
+    pre.fields = fields;
+    pre.step = s->step;
+    const uint32_t counts[2] = {s->pop[0].n, s->pop[1].n};
+    bool ok = std::fwrite(&pre, sizeof(pre), 1, f) == 1 && std::fwrite(counts, sizeof(counts), 1, f) == 1;
+    auto put = [&](const void* p, size_t n) {
+        if (ok && n) ok = std::fwrite(p, 1, n, f) == n;
+    };
+    for (int q = 0; q < 2; ++q) {
+        put(a[q].ids.data(), 4 * a[q].ids.size());
+        put(a[q].x.data(), 4 * a[q].x.size());
+        put(a[q].v.data(), 4 * a[q].v.size());
+        put(a[q].lambda.data(), 4 * a[q].lambda.size());
+        put(a[q].state.data(), 4 * a[q].state.size());
+    }
+    if (std::fclose(f) != 0) ok = false;
+    return ok ? SPH_OK : fail(SPH_E_IO, "sph2_write_frame: write failed");
+}
 
 }  // extern "C"

@@ -15,11 +15,12 @@ ABI; errors raise SphError (the reference throws std::runtime_error).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
 
-from . import _abi
+from . import _abi, state_io
 from ._abi import check, fptr, lib, sph_config, sph_grid, uptr
 
 ORDER = {"sorted": _abi.SPH_ORDER_SORTED, "by_id": _abi.SPH_ORDER_BY_ID}
@@ -232,6 +233,42 @@ class Solver:
 
     def debug_force_lookback_timeout(self, on: bool) -> None:
         check(lib().sph_debug_force_lookback_timeout(self._h, 1 if on else 0))
+
+    # ---- headless state I/O (state_io.py describes the formats) ----
+    @property
+    def step_count(self) -> int:
+        v = C.c_uint64()
+        check(lib().sph_step_count(self._h, C.byref(v)))
+        return v.value
+
+    def save_state(self, path=None) -> bytes:
+        """The complete state as bytes; also written atomically to `path` if given."""
+        need = C.c_uint64()
+        check(lib().sph_save_state(self._h, None, 0, C.byref(need)))
+        buf = (C.c_ubyte * need.value)()
+        check(lib().sph_save_state(self._h, buf, need.value, C.byref(need)))
+        data = bytes(buf)
+        if path is not None:
+            state_io.write_bytes(path, data)
+        return data
+
+    @classmethod
+    def from_state(cls, src) -> "Solver":
+        """Resumes from bytes or a file written by save_state."""
+        data = state_io.read_bytes(src)
+        h = C.c_void_p()
+        check(lib().sph_create_from_state(data, len(data), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self.config = sph_config.from_buffer_copy(data, 24)
+        nf, nb = C.c_uint32(), C.c_uint32()
+        check(lib().sph_counts(h, C.byref(nf), C.byref(nb)))
+        self.num_fluid, self.num_boundary = nf.value, nb.value
+        return self
+
+    def write_frame(self, path, fields=state_io.FIELD_POSITIONS | state_io.FIELD_DENSITIES,
+                    append: bool = True) -> None:
+        check(lib().sph_write_frame(self._h, os.fsencode(path), int(fields), 1 if append else 0))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -9,10 +9,11 @@ Everything runs in libsph2s.so through the C ABI (sph2_* entry points).
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
-from . import _abi
+from . import _abi, state_io
 from ._abi import check, fptr, lib, sph_config2, sph_grid, uptr
 
 LOW, HIGH = 0, 1
@@ -111,6 +112,38 @@ class Solver2:
                                            fptr(r["acc"]), uptr(r["nbr_same"]),
                                            uptr(r["nbr_compl"]), uptr(r["nbr_boundary"])))
         return r
+
+    # ---- headless state I/O (state_io.py describes the formats) ----
+    @property
+    def step_count(self) -> int:
+        v = C.c_uint64()
+        check(lib().sph2_step_count(self._h, C.byref(v)))
+        return v.value
+
+    def save_state(self, path=None) -> bytes:
+        """The complete two-scale state as bytes; also written atomically to `path`."""
+        need = C.c_uint64()
+        check(lib().sph2_save_state(self._h, None, 0, C.byref(need)))
+        buf = (C.c_ubyte * need.value)()
+        check(lib().sph2_save_state(self._h, buf, need.value, C.byref(need)))
+        data = bytes(buf)
+        if path is not None:
+            state_io.write_bytes(path, data)
+        return data
+
+    @classmethod
+    def from_state(cls, src) -> "Solver2":
+        data = state_io.read_bytes(src)
+        h = C.c_void_p()
+        check(lib().sph2_create_from_state(data, len(data), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self.config = sph_config2.from_buffer_copy(data, 24)
+        return self
+
+    def write_frame(self, path, fields=state_io.FIELD_POSITIONS | state_io.FIELD_BLEND,
+                    append: bool = True) -> None:
+        check(lib().sph2_write_frame(self._h, os.fsencode(path), int(fields), 1 if append else 0))
 
     def close(self) -> None:
         if getattr(self, "_h", None):
