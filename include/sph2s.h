@@ -56,7 +56,7 @@ typedef struct sph_config {
     float viscosity;              /* mu */
     float speed_sound;            /* c, boundary force 0.02 c^2 */
     float tension_coefficient;    /* sigma */
-    float xsph_coeff;             /* epsilon (kept for layout; the step does not use it) */
+    float xsph_coeff;             /* epsilon of the XSPH integrator (SPH_INTEGRATOR_XSPH) */
     sph_grid grid;                /* uniform grid, spacing normally h */
 } sph_config;
 
@@ -129,6 +129,17 @@ int sph_destroy(sph_solver* s);
 #define SPH_FIELD_VELOCITIES 2u
 #define SPH_FIELD_DENSITIES 4u /* single scale only */
 #define SPH_FIELD_BLEND 8u     /* two scale only: blend coefficient and state bits */
+
+/* Integrators.  SYMPLECTIC_EULER is the reference's integrateD
+ * (SPH2S_FINAL_SINGLE_SCALE/Solver.cu:713-755), the default.  XSPH is its
+ * integrateXSPHD (Solver.cu:757-853, launch commented out at 1185-1196):
+ * v' = v + dt a; v'' = v' + eps sum_j (v'_j - v'_i) m/rho_j W_poly6; x' = x + dt v''
+ * with eps = sph_config.xsph_coeff, the correction applied per component (the
+ * reference adds its x component to all three).  The differentiable rollout
+ * always uses SYMPLECTIC_EULER. */
+#define SPH_INTEGRATOR_SYMPLECTIC_EULER 0
+#define SPH_INTEGRATOR_XSPH 1
+int sph_set_integrator(sph_solver* s, int32_t integrator);
 
 /* Steps advanced since creation (a state carries it across save / resume). */
 int sph_step_count(sph_solver* s, uint64_t* steps);

@@ -40,6 +40,8 @@ def lib():
         l.or_stencil.argtypes = [C.c_void_p, _f, C.c_uint32, C.c_float, _i, _i]
         l.or_neighborhood.argtypes = [C.c_void_p, _f, C.c_uint32, _u, _u, _u, _u]
         l.or_ss_fields.argtypes = [C.c_void_p, _f, _f, C.c_uint32, _f, C.c_uint32, _d, _d, _u, _u]
+        l.or_ss_xsph_step.argtypes = [C.c_void_p, _f, _f, C.c_uint32, _f, C.c_uint32, C.c_double,
+                                      C.c_double, _d, _d]
         l.or_ss_create.restype = C.c_void_p
         l.or_ss_create.argtypes = [C.c_void_p, _f, C.c_uint32, _f, C.c_uint32, _f]
         l.or_ss_advance.argtypes = [C.c_void_p, C.c_double, C.c_int]
@@ -110,6 +112,20 @@ def ss_fields(config, fluid_xyz, fluid_vel, boundary_xyz):
     lib().or_ss_fields(C.byref(config), _ptr(x, _f), _ptr(v, _f), n, _ptr(b, _f), b.shape[0],
                        _ptr(rho, _d), _ptr(acc, _d), _ptr(nf, _u), _ptr(nb, _u))
     return {"rho": rho, "acc": acc, "nbr_fluid": nf, "nbr_boundary": nb}
+
+
+def ss_xsph_step(config, fluid_xyz, fluid_vel, boundary_xyz, dt, eps):
+    """One XSPH-integrator step (Solver.cu:757-853, per-component correction) from
+    one state; next positions and velocities in input order (float64)."""
+    x = f32(fluid_xyz)
+    v = None if fluid_vel is None else f32(fluid_vel)
+    b = f32(boundary_xyz)
+    n = x.shape[0]
+    xo = np.empty((n, 3), np.float64)
+    vo = np.empty((n, 3), np.float64)
+    lib().or_ss_xsph_step(C.byref(config), _ptr(x, _f), _ptr(v, _f), n, _ptr(b, _f), b.shape[0],
+                          dt, eps, _ptr(xo, _d), _ptr(vo, _d))
+    return xo, vo
 
 
 class SSRollout:

@@ -290,6 +290,55 @@ void or_ss_fields(const OConfig* C, const float* fxyz, const float* fvel, uint32
     }
 }
 
+// One step with the XSPH integrator from a float state (any order; outputs in
+// that order): integrateXSPHD + computeVelXSPHCell, SPH2S_FINAL_SINGLE_SCALE/
+// Solver.cu:345-395, 757-853, with the velocity correction applied per
+// component (the reference adds its x component to all three):
+//   v' = v + dt a,  v'' = v' + eps sum_{r<h} (v'_j - v'_i) m/rho_j W(r),  x' = x + dt v''.
+void or_ss_xsph_step(const OConfig* C, const float* fxyz, const float* fvel, uint32_t n,
+                     const float* bxyz, uint32_t nb, double dt, double eps, double* x_out,
+                     double* v_out) {
+    Boundary B;
+    make_boundary(C->grid, bxyz, nb, B);
+    SortedSet s;
+    sort_set(C->grid, fxyz, n, s);
+    std::vector<float> xs(3 * (size_t)n);
+    std::vector<double> xd(3 * (size_t)n), vd(3 * (size_t)n);
+    for (uint32_t k = 0; k < n; ++k)
+        for (int a = 0; a < 3; ++a) {
+            xs[3 * k + a] = fxyz[3 * s.perm[k] + a];
+            xd[3 * k + a] = (double)xs[3 * k + a];
+            vd[3 * k + a] = fvel ? (double)fvel[3 * s.perm[k] + a] : 0.0;
+        }
+    std::vector<double> rho, acc;
+    fields_sorted(*C, xs, xd, vd, s.cells, B, rho, acc, nullptr, nullptr);
+    std::vector<double> vp(3 * (size_t)n);
+    for (size_t k = 0; k < 3 * (size_t)n; ++k) vp[k] = vd[k] + dt * acc[k];
+    const float h = C->effective_radius;
+    const float T = thresh_sq(h);
+    const Kern K((double)h);
+    const double m = C->fluid_particle_mass;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)n; ++i) {
+        const float* xi = &xs[3 * i];
+        double sum[3] = {0, 0, 0};
+        for_stencil(C->grid, s.cells, xi, h, [&](uint32_t j) {
+            if (r2_f32(xi, &xs[3 * j]) < T) {
+                double dx = xd[3 * i] - xd[3 * j], dy = xd[3 * i + 1] - xd[3 * j + 1],
+                       dz = xd[3 * i + 2] - xd[3 * j + 2];
+                const double w = K.W(std::sqrt(dx * dx + dy * dy + dz * dz)) * m / rho[j];
+                for (int a = 0; a < 3; ++a) sum[a] += (vp[3 * j + a] - vp[3 * i + a]) * w;
+            }
+        });
+        const uint32_t q = s.perm[i];
+        for (int a = 0; a < 3; ++a) {
+            const double v2 = vp[3 * i + a] + eps * sum[a];
+            v_out[3 * q + a] = v2;
+            x_out[3 * q + a] = xd[3 * i + a] + dt * v2;
+        }
+    }
+}
+
 // ---- rollout handle (state in double, sorted order after every step) --------
 
 void* or_ss_create(const OConfig* C, const float* fxyz, uint32_t n, const float* bxyz,

@@ -135,6 +135,7 @@ SIGNATURES = {
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_uint32, C.c_int32, C.c_void_p]),
+    "sph_set_integrator": (C.c_int, [_vp, C.c_int32]),
     "sph_step_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
     "sph_save_state": (C.c_int, [_vp, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "sph_create_from_state": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(_vp)]),

@@ -27,7 +27,7 @@ int free_solver(sph_solver* s) {
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->err,     s->stage, s->nbr, s->nbr_count,
-                    s->bnear,   s->pos0};
+                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->err_host) cudaFreeHost(s->err_host);
@@ -79,8 +79,38 @@ void enqueue_force(sph_solver* s, float dt) {
 void enqueue_step(sph_solver* s, float dt) {
     if (s->n == 0) return;
     enqueue_neighborhood(s);
+    if (s->integrator == SPH_INTEGRATOR_XSPH) {
+        // density (+ full neighbour counts), accelerations, XSPH integrate
+        density_kernel<true><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
+            s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, s->xall);
+        force_kernel<1><<<blocks_for(s->n), 256, 0, s->stream>>>(
+            s->spos, s->svel, s->aux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
+            s->n, s->nb, s->P, dt, nullptr, nullptr, s->xacc, s->xnb);
+        xsph_integrate_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(
+            s->spos, s->svel, s->xacc, s->aux, s->cells, s->nbr, s->nbr_count, s->xall, s->n, s->P,
+            dt, s->cfg.xsph_coeff, s->pos, s->vel);
+        return;
+    }
     enqueue_density(s);
     enqueue_force(s, dt);
+}
+
+int set_integrator(sph_solver* s, int32_t integrator) {
+    if (integrator != SPH_INTEGRATOR_SYMPLECTIC_EULER && integrator != SPH_INTEGRATOR_XSPH)
+        return fail(SPH_E_INVALID, "sph_set_integrator: unknown integrator");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (integrator == SPH_INTEGRATOR_XSPH && !s->xacc) {
+        const size_t n = s->n ? s->n : 1;
+        SPH_CUDA(cudaMalloc(&s->xacc, 12 * n));
+        SPH_CUDA(cudaMalloc(&s->xall, 4 * n));
+        SPH_CUDA(cudaMalloc(&s->xnb, 4 * n));
+    }
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    s->integrator = integrator;
+    return SPH_OK;
 }
 
 int check_device_error(sph_solver* s) {
@@ -340,6 +370,11 @@ int sph_set_velocities(sph_solver* s, const float* xyz, int32_t order) {
     }
     SPH_CUDA(cudaMemcpy(s->vel, v.data(), sizeof(float4) * s->n, cudaMemcpyHostToDevice));
     return SPH_OK;
+}
+
+int sph_set_integrator(sph_solver* s, int32_t integrator) {
+    if (!s) return fail(SPH_E_INVALID, "sph_set_integrator: NULL handle");
+    return set_integrator(s, integrator);
 }
 
 int sph_counts(sph_solver* s, uint32_t* n_fluid, uint32_t* n_boundary) {

@@ -120,4 +120,5 @@ static __global__ void __launch_bounds__(256) boundary_near_kernel(const uint2* 
 }  // namespace sph
 
 #include "density_kernel.cuh"
+#include "xsph_kernel.cuh"
 #include "force_kernel.cuh"

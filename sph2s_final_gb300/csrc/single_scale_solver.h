@@ -40,6 +40,10 @@ struct sph_solver {
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.0f;
     uint64_t step = 0;  // steps advanced since creation (carried by saved states)
+    int32_t integrator = SPH_INTEGRATOR_SYMPLECTIC_EULER;
+    float* xacc = nullptr;     // XSPH integrator: accelerations of the step (3 per particle)
+    uint32_t* xall = nullptr;  // XSPH integrator: neighbours incl. distance 0, per particle
+    uint32_t* xnb = nullptr;   // XSPH integrator: boundary neighbour counts (unused output)
     sph::Rollout* rollout = nullptr;
 };
 
@@ -50,6 +54,9 @@ int enqueue_neighborhood(sph_solver* s);
 void enqueue_density(sph_solver* s);
 void enqueue_force(sph_solver* s, float dt);
 int check_device_error(sph_solver* s);
+// Selects the integrator (allocating the XSPH buffers on first use) and drops
+// the captured step graph.
+int set_integrator(sph_solver* s, int32_t integrator);
 // Creates a handle from host float4 arrays: fluid positions (persistent id in
 // w) and velocities in the order the next step starts from, creation-time
 // positions (rollout restarts), boundary positions (presorted here).

@@ -2,7 +2,7 @@
 // single-scale handle (formats in state_format.h).
 //
 // Single-scale state body:
-//   sph_config (64 B) | u32 n | u32 nb |
+//   sph_config (64 B) | u32 n | u32 nb | u32 integrator | u32 reserved (0) |
 //   float4 pos[n]   positions in the sorted order of the last step, persistent id in w
 //   float4 vel[n]   velocities, same order
 //   float4 pos0[n]  positions at creation, creation order (rollout restarts)
@@ -24,7 +24,7 @@ using namespace sph_io;
 namespace {
 
 uint64_t ss_state_bytes(uint64_t n, uint64_t nb) {
-    return sizeof(StatePrefix) + sizeof(sph_config) + 8 + 16 * (3 * n + nb) + 8;
+    return sizeof(StatePrefix) + sizeof(sph_config) + 16 + 16 * (3 * n + nb) + 8;
 }
 
 // Every w of pos must be a distinct id below n.
@@ -69,8 +69,8 @@ int sph_save_state(sph_solver* s, void* dst, uint64_t capacity, uint64_t* bytes)
     pre.step = s->step;
     w.put(&pre, sizeof(pre));
     w.put(&s->cfg, sizeof(sph_config));
-    w.put(&s->n, 4);
-    w.put(&s->nb, 4);
+    const uint32_t counts[4] = {s->n, s->nb, (uint32_t)s->integrator, 0u};
+    w.put(counts, sizeof(counts));
     const float4* src[3] = {s->pos, s->vel, s->pos0};
     for (const float4* a : src)
         if (s->n) SPH_CUDA(cudaMemcpy(w.take(16 * (size_t)s->n), a, 16 * (size_t)s->n, cudaMemcpyDeviceToHost));
@@ -88,9 +88,13 @@ int sph_create_from_state(const void* src, uint64_t bytes, sph_solver** out) {
         return fail(SPH_E_INVALID, "sph_create_from_state: not a single-scale state, or corrupt");
     Reader r{static_cast<const unsigned char*>(src), (size_t)bytes - 8, sizeof(StatePrefix)};
     sph_config cfg;
-    uint32_t n = 0, nb = 0;
-    if (!r.get(&cfg, sizeof(cfg)) || !r.get(&n, 4) || !r.get(&nb, 4))
+    uint32_t c[4];
+    if (!r.get(&cfg, sizeof(cfg)) || !r.get(c, sizeof(c)))
         return fail(SPH_E_INVALID, "sph_create_from_state: truncated header");
+    const uint32_t n = c[0], nb = c[1];
+    const int32_t integrator = (int32_t)c[2];
+    if (integrator != SPH_INTEGRATOR_SYMPLECTIC_EULER && integrator != SPH_INTEGRATOR_XSPH)
+        return fail(SPH_E_INVALID, "sph_create_from_state: unknown integrator");
     if (n > kMaxParticles || nb > kMaxParticles)
         return fail(SPH_E_CAPACITY, "sph_create_from_state: more than 2^30 particles");
     if (bytes != ss_state_bytes(n, nb))
@@ -102,8 +106,16 @@ int sph_create_from_state(const void* src, uint64_t bytes, sph_solver** out) {
     r.get(bpos.data(), 16 * (size_t)nb);
     if (!ids_are_permutation(pos))
         return fail(SPH_E_INVALID, "sph_create_from_state: persistent ids are not a permutation");
-    return sph_ss::create_solver(&cfg, pos.data(), vel.data(), pos0.data(), n, bpos.data(), nb,
-                                 pre.step, out);
+    int rc = sph_ss::create_solver(&cfg, pos.data(), vel.data(), pos0.data(), n, bpos.data(), nb,
+                                   pre.step, out);
+    if (rc == SPH_OK && integrator != SPH_INTEGRATOR_SYMPLECTIC_EULER) {
+        rc = sph_ss::set_integrator(*out, integrator);
+        if (rc != SPH_OK) {
+            sph_destroy(*out);
+            *out = nullptr;
+        }
+    }
+    return rc;
 }
 
 int sph_write_frame(sph_solver* s, const char* path, uint32_t fields, int32_t append) {

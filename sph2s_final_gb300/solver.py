@@ -24,6 +24,7 @@ from . import _abi, state_io
 from ._abi import check, fptr, lib, sph_config, sph_grid, uptr
 
 ORDER = {"sorted": _abi.SPH_ORDER_SORTED, "by_id": _abi.SPH_ORDER_BY_ID}
+INTEGRATORS = {"symplectic_euler": 0, "xsph": 1}
 
 
 class Grid:
@@ -233,6 +234,11 @@ class Solver:
 
     def debug_force_lookback_timeout(self, on: bool) -> None:
         check(lib().sph_debug_force_lookback_timeout(self._h, 1 if on else 0))
+
+    def set_integrator(self, integrator: str) -> None:
+        """"symplectic_euler" (integrateD, the default) or "xsph" (integrateXSPHD,
+        Solver.cu:757-853, per-component correction, eps = config.xsph_coeff)."""
+        check(lib().sph_set_integrator(self._h, INTEGRATORS[integrator]))
 
     # ---- headless state I/O (state_io.py describes the formats) ----
     @property

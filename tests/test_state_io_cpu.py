@@ -31,7 +31,7 @@ def single_scale_state(ids, nb=2, step=7, version=1):
     vel = np.zeros((n, 4), np.float32)
     bpos = rng.uniform(0.0, 1.0, (nb, 4)).astype(np.float32)
     body = (b"SPHSTAT1" + struct.pack("<IIQ", version, 1, step)
-            + C.string_at(C.addressof(cfg), C.sizeof(cfg)) + struct.pack("<II", n, nb)
+            + C.string_at(C.addressof(cfg), C.sizeof(cfg)) + struct.pack("<IIII", n, nb, 0, 0)
             + pos.tobytes() + vel.tobytes() + pos.tobytes() + bpos.tobytes())
     return body + struct.pack("<Q", word_fnv1a(body))
 
