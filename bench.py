@@ -278,6 +278,65 @@ def measure_adjoint(steps: int = 200, every: int = 20, reps: int = 3):
             "loss": loss, "timing": "host clock around synchronous calls, best of 3"}
 
 
+def measure_batched_adjoint(num: int = 64, steps: int = 100, every: int = 20, reps: int = 2):
+    """Batched differentiable rollout over the first `num` scenes of the 256-scene
+    batch: forward (checkpoints), per-scene splat loss on a 32^3 node grid, and
+    backward, against the same rollouts run scene after scene by single-scale
+    solvers.  Host clock around synchronous calls, best of `reps`."""
+    import torch
+
+    from sph2s_final_gb300 import scenes
+    from sph2s_final_gb300.autograd import node_grid
+    from sph2s_final_gb300.batched import Batch
+    from sph2s_final_gb300.solver import Solver
+
+    scs = scenes.batched_scenes()[:num]
+    dt = scs[0].dt
+    n = sum(s.fluid.num_particles for s in scs)
+    rng = np.random.default_rng(1)
+    vt = [rng.normal(0.0, 0.1, (s.fluid.num_particles, 3)).astype(np.float32) for s in scs]
+    v0 = [np.zeros_like(v) for v in vt]
+    mu = np.array([s.config.viscosity for s in scs], np.float32)
+    nodes = [node_grid() for _ in scs]
+    with Batch([(s.fluid.positions, s.boundary.positions, s.config) for s in scs]) as b:
+        b.autotune(dt)
+        b.rollout_forward(vt, mu, dt, steps, every)
+        targets, _ = b.rollout_density_loss(nodes)
+        fw, bw = [], []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.rollout_forward(v0, mu, dt, steps, every)
+            b.rollout_density_loss(nodes, targets)
+            t1 = time.perf_counter()
+            b.rollout_backward()
+            fw.append(t1 - t0)
+            bw.append(time.perf_counter() - t1)
+    solvers = [Solver(s.fluid, s.boundary, s.config) for s in scs]
+
+    def serial_pass():
+        for k, so in enumerate(solvers):
+            so.rollout_forward(v0[k], float(mu[k]), dt, steps, every)
+            so.rollout_density_loss(nodes[k], targets[k])
+            so.rollout_backward()
+
+    serial_pass()  # allocates every solver's tape
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    serial_pass()
+    serial = time.perf_counter() - t0
+    for so in solvers:
+        so.close()
+    f, bk = min(fw), min(bw)
+    return {"scenes": num, "fluid_particles": n, "steps": steps, "checkpoint_every": every,
+            "forward_and_loss_ms": 1e3 * f, "backward_ms": 1e3 * bk,
+            "adjoint_over_forward": bk / f,
+            "per_scene_serial_ms": 1e3 * serial, "speedup": serial / (f + bk),
+            "timing": "host clock around synchronous calls; batched best of 2; per-scene "
+                      "solvers (tapes allocated in an untimed pass) run forward, loss and "
+                      "backward one scene after another"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -441,6 +500,7 @@ def run_ours(args):
     if ws == 1 and not args.no_extras:
         line["batched"] = measure_batched(args.batched_steps)
         line["adjoint"] = measure_adjoint()
+        line["batched_adjoint"] = measure_batched_adjoint()
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -318,6 +318,22 @@ int sphb_get_scene(sph_batch* b, uint32_t scene, float* xyz, float* vel, float* 
 int sphb_autotune(sph_batch* b, float dt, int32_t* choice3);
 int sphb_destroy(sph_batch* b);
 
+/* Batched differentiable rollout (no counterpart in the reference): the
+ * sph_rollout_* sequence for every scene of the batch at once, through the
+ * batch's packed arrays and one launch per kernel.  Arrays are packed by
+ * scene in scene order, each scene's particles in creation order:
+ *   v0_xyz, grad_v0, grad_x0   3 floats per particle (all scenes)
+ *   viscosity, loss, grad_mu   one value per scene (viscosity NULL = keep)
+ *   nodes                      one node grid per scene
+ *   target, field              the scenes' node values, concatenated
+ * Each scene's loss, fields and gradients equal those of a single-scale
+ * solver on that scene. */
+int sphb_rollout_forward(sph_batch* b, const float* v0_xyz, const float* viscosity, float dt,
+                         int32_t steps, int32_t checkpoint_every);
+int sphb_rollout_density_loss(sph_batch* b, const sph_grid* nodes, const float* target,
+                              float* field, double* loss);
+int sphb_rollout_backward(sph_batch* b, float* grad_v0, float* grad_x0, double* grad_mu);
+
 /* ---- key-value sort ------------------------------------------------------ */
 
 /* Stable ascending sort of n (uint32 key, uint32 value) pairs in device

@@ -131,6 +131,10 @@ SIGNATURES = {
     "sphb_get_scene": (C.c_int, [_vp, C.c_uint32, _f, _f, _f, C.c_int32]),
     "sphb_autotune": (C.c_int, [_vp, C.c_float, C.POINTER(C.c_int32)]),
     "sphb_destroy": (C.c_int, [_vp]),
+    "sphb_rollout_forward": (C.c_int, [_vp, _f, _f, C.c_float, C.c_int32, C.c_int32]),
+    "sphb_rollout_density_loss": (C.c_int, [_vp, C.POINTER(sph_grid), _f, _f,
+                                            C.POINTER(C.c_double)]),
+    "sphb_rollout_backward": (C.c_int, [_vp, _f, _f, C.POINTER(C.c_double)]),
     "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -134,20 +134,20 @@ struct AdjForcePair {
     }
 };
 
-// Adjoint of force + integrate for particle i of the step's sorted order.
-static __global__ void __launch_bounds__(256) adj_force_kernel(
-    const float4* __restrict__ pos, const float4* __restrict__ vel, const float* __restrict__ rho,
-    const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
+// Adjoint of force + integrate for particle i of the step's sorted order;
+// returns particle i's share of d L / d mu.  cells/bcells/bnear are the
+// particle's own grid tables (the batched rollout passes per-scene tables, P
+// and mu).
+__device__ __forceinline__ float adj_force_one(
+    uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel,
+    const float* __restrict__ rho, const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
-    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, SimParams P, float mu, float dt,
-    const float4* __restrict__ lam, const float4* __restrict__ gx_in,
+    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, const SimParams& P, float mu,
+    float dt, const float4* __restrict__ lam, const float4* __restrict__ gx_in,
     const float4* __restrict__ gv_in, float4* __restrict__ gx_out, float4* __restrict__ gv_out,
-    float* __restrict__ grho, float* __restrict__ gmu_block) {
-    __shared__ float s_red[8];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float gmu_i = 0.0f;
-    if (i < n) {
+    float* __restrict__ grho) {
+    {
         const float4 xi = pos[i];
         AdjForcePair A;
         A.vel = vel;
@@ -217,19 +217,43 @@ static __global__ void __launch_bounds__(256) adj_force_kernel(
         gv_out[i] = make_float4(fmaf(dt, gxi.x, gvi.x) + A.gvx, fmaf(dt, gxi.y, gvi.y) + A.gvy,
                                 fmaf(dt, gxi.z, gvi.z) + A.gvz, 0.f);
         grho[i] = A.grho;
-        gmu_i = A.gmu;
+        return A.gmu;
     }
-    // per-block sum of d L / d mu (reduced in a fixed order afterwards)
-    float v = gmu_i;
+}
+
+// Block sum of one value per thread in a fixed order (warp shuffles, then the
+// warps in index order); the result is valid in thread 0.  Every thread of
+// the block must call it.
+__device__ __forceinline__ float block_sum_fixed(float v) {
+    __shared__ float s_red[32];
 #pragma unroll
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    __syncthreads();
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.0f;
+    float t = 0.0f;
+    if (threadIdx.x == 0)
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w];
-        gmu_block[blockIdx.x] = t;
-    }
+    return t;
+}
+
+static __global__ void __launch_bounds__(256) adj_force_kernel(
+    const float4* __restrict__ pos, const float4* __restrict__ vel, const float* __restrict__ rho,
+    const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
+    const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells,
+    const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
+    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, SimParams P, float mu, float dt,
+    const float4* __restrict__ lam, const float4* __restrict__ gx_in,
+    const float4* __restrict__ gv_in, float4* __restrict__ gx_out, float4* __restrict__ gv_out,
+    float* __restrict__ grho, float* __restrict__ gmu_block) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float gmu_i = 0.0f;
+    if (i < n)
+        gmu_i = adj_force_one(i, pos, vel, rho, aux, nbr4, nbr_count, cells, bpos, bcells, bnear, n,
+                              nb, P, mu, dt, lam, gx_in, gv_in, gx_out, gv_out, grho);
+    // per-block sum of d L / d mu (reduced in a fixed order afterwards)
+    const float t = block_sum_fixed(gmu_i);
+    if (threadIdx.x == 0) gmu_block[blockIdx.x] = t;
 }
 
 struct AdjDensityPair {
@@ -246,12 +270,12 @@ struct AdjDensityPair {
 };
 
 // Density adjoint: gx_i += -6 m C6 sum_j (h^2 - r^2)^2 (grho_i + grho_j) x_ij.
-static __global__ void __launch_bounds__(256) adj_density_kernel(
-    const float4* __restrict__ pos, const uint4* __restrict__ nbr4,
-    const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells, uint32_t n,
-    SimParams P, const float* __restrict__ grho, float4* __restrict__ gx) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void adj_density_one(uint32_t i, const float4* __restrict__ pos,
+                                                const uint4* __restrict__ nbr4,
+                                                const uint32_t* __restrict__ nbr_count,
+                                                const uint2* __restrict__ cells, uint32_t n,
+                                                const SimParams& P, const float* __restrict__ grho,
+                                                float4* __restrict__ gx) {
     const float4 xi = pos[i];
     AdjDensityPair A;
     A.grho = grho;
@@ -265,6 +289,15 @@ static __global__ void __launch_bounds__(256) adj_density_kernel(
     g.y += A.gy;
     g.z += A.gz;
     gx[i] = g;
+}
+
+static __global__ void __launch_bounds__(256) adj_density_kernel(
+    const float4* __restrict__ pos, const uint4* __restrict__ nbr4,
+    const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells, uint32_t n,
+    SimParams P, const float* __restrict__ grho, float4* __restrict__ gx) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    adj_density_one(i, pos, nbr4, nbr_count, cells, n, P, grho, gx);
 }
 
 // Scatter from the step's sorted order back to the order before the sort:
@@ -294,13 +327,9 @@ static __global__ void adj_sum_kernel(const float* __restrict__ part, uint32_t c
 // Poly6 splat of the particles on the cell centres of a node grid:
 // G_n = m C6 sum_i (h^2 - r^2)^3 over r < h (the same stencil rule as the
 // density pass, on the particles' grid).
-static __global__ void __launch_bounds__(256) splat_kernel(const float4* __restrict__ pos,
-                                                           const uint2* __restrict__ cells,
-                                                           uint32_t n, SimParams P, GridParams ng,
-                                                           float* __restrict__ field) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nn = (uint32_t)ng.dx * ng.dy * ng.dz;
-    if (c >= nn) return;
+__device__ __forceinline__ float splat_node(uint32_t c, const float4* __restrict__ pos,
+                                            const uint2* __restrict__ cells, uint32_t n,
+                                            const SimParams& P, const GridParams& ng) {
     const int ix = (int)(c % (uint32_t)ng.dx), iy = (int)((c / (uint32_t)ng.dx) % (uint32_t)ng.dy),
               iz = (int)(c / ((uint32_t)ng.dx * ng.dy));
     const float y0 = ng.ox + ((float)ix + 0.5f) * ng.spacing;
@@ -325,19 +354,24 @@ static __global__ void __launch_bounds__(256) splat_kernel(const float4* __restr
                 }
             }
         }
-    field[c] = P.dens_coef * sum;
+    return P.dens_coef * sum;
+}
+
+static __global__ void __launch_bounds__(256) splat_kernel(const float4* __restrict__ pos,
+                                                           const uint2* __restrict__ cells,
+                                                           uint32_t n, SimParams P, GridParams ng,
+                                                           float* __restrict__ field) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nn = (uint32_t)ng.dx * ng.dy * ng.dz;
+    if (c >= nn) return;
+    field[c] = splat_node(c, pos, cells, n, P, ng);
 }
 
 // dL/dx_i of L = mean_n (G_n - target_n)^2, for the sorted particles:
 // sum over nodes n with |x_i - y_n| < h of (2/N_n) e_n m C6 3 (h^2-r^2)^2 (-2)(x_i - y_n).
-static __global__ void __launch_bounds__(256) splat_grad_kernel(const float4* __restrict__ pos,
-                                                                uint32_t n, SimParams P,
-                                                                GridParams ng,
-                                                                const float* __restrict__ err_n,
-                                                                float scale,
-                                                                float4* __restrict__ gx) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ float4 splat_grad_one(uint32_t i, const float4* __restrict__ pos,
+                                                 const SimParams& P, const GridParams& ng,
+                                                 const float* __restrict__ err_n, float scale) {
     const float4 xi = pos[i];
     const float inv = 1.0f / ng.spacing;
     const int x0 = max(0, (int)ceilf((xi.x - P.h - ng.ox) * inv - 0.5f) - 1);
@@ -371,7 +405,18 @@ static __global__ void __launch_bounds__(256) splat_grad_kernel(const float4* __
                     gzz = fmaf(c, dz, gzz);
                 }
             }
-    gx[i] = make_float4(gxx, gyy, gzz, 0.f);
+    return make_float4(gxx, gyy, gzz, 0.f);
+}
+
+static __global__ void __launch_bounds__(256) splat_grad_kernel(const float4* __restrict__ pos,
+                                                                uint32_t n, SimParams P,
+                                                                GridParams ng,
+                                                                const float* __restrict__ err_n,
+                                                                float scale,
+                                                                float4* __restrict__ gx) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    gx[i] = splat_grad_one(i, pos, P, ng, err_n, scale);
 }
 
 }  // namespace sph

@@ -12,7 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
-#include "batched_kernels.cuh"
+#include "batched_solver.h"
 #include "errors.h"
 #include "host_params.h"
 #include "single_scale_kernels.cuh"
@@ -20,8 +20,6 @@
 using namespace sph;
 
 namespace {
-
-constexpr int kBlockChoices[3] = {128, 256, 512};
 
 template <class T>
 int dalloc(T** p, size_t count, std::vector<void*>& owned) {
@@ -32,45 +30,12 @@ int dalloc(T** p, size_t count, std::vector<void*>& owned) {
 
 }  // namespace
 
-struct sph_batch {
-    uint32_t S = 0;                  // scenes
-    uint32_t N = 0, NB = 0, NC = 0;  // fluid, boundary, cells (all scenes)
-    int shift = 0, passes = 0, bpasses = 0;
-    std::vector<SceneRec> recs_h;
-    SceneRec* recs = nullptr;
-    cudaStream_t stream = nullptr;
-    float4 *pos = nullptr, *vel = nullptr, *spos = nullptr, *svel = nullptr;
-    float* rho = nullptr;
-    float2* aux = nullptr;
-    uint4* nbr = nullptr;
-    uint32_t* nbr_count = nullptr;
-    uint32_t* keys[2] = {nullptr, nullptr};
-    uint32_t* vals[2] = {nullptr, nullptr};
-    uint2 *cells = nullptr, *bcells = nullptr;
-    uint8_t* bnear = nullptr;
-    float4* bpos = nullptr;
-    void* sort_mem = nullptr;
-    SortScratch sort;
-    uint32_t* err = nullptr;
-    uint32_t* err_host = nullptr;
-    // tiles per block-size choice (fluid), boundary tiles at 256
-    uint2* tiles[3] = {nullptr, nullptr, nullptr};
-    uint32_t ntiles[3] = {0, 0, 0};
-    uint2* btiles = nullptr;
-    uint32_t nbtiles = 0;
-    int bs_density = 1, bs_force = 1;  // index into kBlockChoices
-    int grid_mult = 4;                 // persistent grid = grid_mult * SMs
-    int sms = 152;
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = 0.0f;
-    std::vector<void*> owned;
-};
-
-namespace {
+namespace sph_b {
 
 int free_batch(sph_batch* b) {
     if (!b) return SPH_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    sphb_rollout_release(b);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (void* p : b->owned) cudaFree(p);
     if (b->err_host) cudaFreeHost(b->err_host);
@@ -124,7 +89,7 @@ void enqueue_force(sph_batch* b, float dt) {
     }
 }
 
-void enqueue_neighborhood(sph_batch* b) {
+int enqueue_neighborhood(sph_batch* b) {
     cudaStream_t st = b->stream;
     cudaMemsetAsync(b->cells, 0xFF, sizeof(uint2) * b->NC, st);
     sort_reset(b->sort, st);
@@ -136,6 +101,7 @@ void enqueue_neighborhood(sph_batch* b) {
     b_gather_cells_kernel<256, true><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
         b->tiles[1], b->ntiles[1], b->recs, b->keys[o], b->vals[o], b->N, b->shift, false, b->pos,
         b->vel, b->spos, b->svel, b->cells, b->err);
+    return o;
 }
 
 void enqueue_step(sph_batch* b, float dt) {
@@ -143,6 +109,17 @@ void enqueue_step(sph_batch* b, float dt) {
     enqueue_neighborhood(b);
     enqueue_density(b);
     enqueue_force(b, dt);
+}
+
+int refresh_scene_params(sph_batch* b) {
+    for (uint32_t s = 0; s < b->S; ++s) {
+        int rc = make_sim_params(b->cfgs[s], &b->recs_h[s].P);
+        if (rc != SPH_OK) return rc;
+    }
+    SPH_CUDA(cudaMemcpyAsync(b->recs, b->recs_h.data(), sizeof(SceneRec) * b->S,
+                             cudaMemcpyHostToDevice, b->stream));
+    SPH_CUDA(cudaStreamSynchronize(b->stream));
+    return SPH_OK;
 }
 
 int check_err(sph_batch* b) {
@@ -158,7 +135,9 @@ int check_err(sph_batch* b) {
     return SPH_OK;
 }
 
-}  // namespace
+}  // namespace sph_b
+
+using namespace sph_b;
 
 extern "C" {
 
@@ -192,6 +171,8 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
         NC += sph_grid_num_cells(&d.config.grid);
         maxbits = std::max(maxbits, R.P.g.mbits);
         b->recs_h.push_back(R);
+        b->cfgs.push_back(d.config);
+        b->tile_first.push_back(0);
     }
     int sbits = 1;
     while ((1u << sbits) < num_scenes) ++sbits;
@@ -244,6 +225,8 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(check_cuda(cudaMemset(b->err, 0, 4), "memset", __FILE__, __LINE__));
     TRY(check_cuda(cudaMallocHost((void**)&b->err_host, 4), "pinned", __FILE__, __LINE__));
     TRY(check_cuda(cudaMemcpy(b->recs, b->recs_h.data(), sizeof(SceneRec) * num_scenes, cudaMemcpyHostToDevice), "recs", __FILE__, __LINE__));
+    for (uint32_t s = 1; s < num_scenes; ++s)
+        b->tile_first[s] = b->tile_first[s - 1] + (b->recs_h[s - 1].p_n + 255u) / 256u;
     for (int k = 0; k < 3; ++k) {
         std::vector<uint2> t = make_tiles(b->recs_h, kBlockChoices[k], false);
         b->ntiles[k] = (uint32_t)t.size();
@@ -279,7 +262,9 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
                 hb[R.b_off + i] = make_float4(x[0], x[1], x[2], w);
             }
         }
+        TRY(dalloc(&b->pos0, b->N, b->owned));
         if (b->N) {
+            TRY(check_cuda(cudaMemcpy(b->pos0, hp.data(), 16 * (size_t)b->N, cudaMemcpyHostToDevice), "upload", __FILE__, __LINE__));
             TRY(check_cuda(cudaMemcpy(b->pos, hp.data(), 16 * (size_t)b->N, cudaMemcpyHostToDevice), "upload", __FILE__, __LINE__));
             TRY(check_cuda(cudaMemcpy(b->vel, hv.data(), 16 * (size_t)b->N, cudaMemcpyHostToDevice), "upload", __FILE__, __LINE__));
         }
