@@ -223,9 +223,30 @@ typedef struct sph_config2 {
     float tension_coefficient;
     float blend_increment;        /* lambda change per step (BlendIncrement) */
     sph_grid grid[2];             /* one grid per population, spacing = its support */
-    int32_t refine_axis;          /* 0, 1, 2 or -1 */
+    int32_t refine_axis;          /* slab trigger: 0, 1, 2 or -1 (no slab) */
     float refine_lo, refine_hi;
+    int32_t mode;                 /* SPH2_MODE_BLENDED or SPH2_MODE_COUPLED */
+    int32_t split_trigger;        /* SPH2_SPLIT_SLAB or SPH2_SPLIT_SURFACE */
+    float surface_density;        /* SPH2_SPLIT_SURFACE: a particle with rho < this is at the surface */
 } sph_config2;
+
+/* Modes.  BLENDED is SPH2S_FINAL_TWO_SCALE: lambda-weighted sums, velocity
+ * clamp, fade / split / merge state machine.  COUPLED is
+ * SPH2S_FINAL_TWO_SCALE_COUPLED (Solver.cu:648-1015): two fixed populations,
+ * unweighted sums, no clamp, no state changes, and its complementary tension
+ * weight W_{h_c}(r) of the neighbour's own support (Solver.cu:448-460). */
+#define SPH2_MODE_BLENDED 0
+#define SPH2_MODE_COUPLED 1
+/* Split triggers (BLENDED).  SLAB: a LOW particle whose start-of-step
+ * position lies inside refine_lo < x[refine_axis] < refine_hi splits; a group
+ * whose centroid leaves the slab merges.  SURFACE replaces the reference's
+ * render-pass surface flag (getSurfaceIDs, SPH2S_FINAL_TWO_SCALE/SSFRenderer.cu:
+ * 196-218, which sets state bit 8) and its commented-out split marking
+ * (Solver.cu:1077-1082) by a density deficit computed in the step: a normal
+ * LOW particle with rho < surface_density splits; a group whose 8 members
+ * are fully blended in and all have rho >= surface_density merges. */
+#define SPH2_SPLIT_SLAB 0
+#define SPH2_SPLIT_SURFACE 1
 
 typedef struct sph_solver2 sph_solver2;
 
@@ -270,6 +291,17 @@ int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sor
                            float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
                            uint32_t* nbr_boundary);
 int sph2_destroy(sph_solver2* s);
+/* Colour / energy output of the two-scale force pass (dColorValues,
+ * SPH2S_FINAL_TWO_SCALE/Solver.cu:206-213, 378-387, 897-907, 1050-1070): per
+ * particle, over its own population, e = |sum_j psi_ij v_j|^2 / ((sum_j psi_ij)^2 h)
+ * with the Mexican-hat wavelet psi (self included), colour = 0.3 if the
+ * particle is within 0.0025 of its neighbours' mass centre, else min(e, 300)/300.
+ * Off by default; when on, every step writes it.  sph2_get_colors returns the
+ * last step's values in that step's sorted order with the persistent ids
+ * (*count = particles of that step; any pointer may be NULL). */
+int sph2_set_color_output(sph_solver2* s, int32_t on);
+int sph2_get_colors(sph_solver2* s, int32_t population, float* colour, uint32_t* ids_sorted,
+                    uint32_t* count);
 /* Two-scale state I/O, as sph_save_state / sph_create_from_state: both
  * populations with blend coefficients, state bits and group ids, the group
  * and id counters, capacities and the presorted boundary. */

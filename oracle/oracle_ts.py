@@ -27,7 +27,8 @@ def lib():
                                    C.c_uint32, _u]
         l.or_ts_advance.argtypes = [C.c_void_p, C.c_double, C.c_int]
         l.or_ts_step_fields.argtypes = [C.c_void_p, C.c_double, C.POINTER(_d), C.POINTER(_d),
-                                        C.POINTER(_u), C.POINTER(_u), C.POINTER(_u), C.POINTER(_u)]
+                                        C.POINTER(_u), C.POINTER(_u), C.POINTER(_u), C.POINTER(_u),
+                                        C.POINTER(_d), C.POINTER(_d)]
         l.or_ts_counts.argtypes = [C.c_void_p, _u, _u, _u]
         l.or_ts_last_stats.argtypes = [C.c_void_p, _u]
         l.or_ts_get.argtypes = [C.c_void_p, C.c_int, _d, _d, _f, _i, _u, _u]
@@ -81,15 +82,19 @@ class TSRollout:
         """One step; fields of the sorted pre-step populations."""
         c = self.counts()
         n = [c["low"], c["high"]]
-        out = {k: [None, None] for k in ("rho", "acc", "nbr_same", "nbr_compl", "nbr_bnd", "ids")}
+        out = {k: [None, None] for k in ("rho", "acc", "nbr_same", "nbr_compl", "nbr_bnd", "ids",
+                                         "colour", "dist_cm")}
         for r in range(2):
             out["rho"][r] = np.empty(n[r])
             out["acc"][r] = np.empty((n[r], 3))
+            out["colour"][r] = np.empty(n[r])
+            out["dist_cm"][r] = np.empty(n[r])
             for k in ("nbr_same", "nbr_compl", "nbr_bnd", "ids"):
                 out[k][r] = np.empty(n[r], np.uint32)
         lib().or_ts_step_fields(self._h, dt, _pp(out["rho"], _d), _pp(out["acc"], _d),
                                 _pp(out["nbr_same"], _u), _pp(out["nbr_compl"], _u),
-                                _pp(out["nbr_bnd"], _u), _pp(out["ids"], _u))
+                                _pp(out["nbr_bnd"], _u), _pp(out["ids"], _u),
+                                _pp(out["colour"], _d), _pp(out["dist_cm"], _d))
         return out
 
     def last_stats(self):

@@ -37,6 +37,17 @@
 //   * the velocity clamp skips |v| = 0 (the reference divides 0 by 0 there).
 // Blend coefficients and the state machine run in FP32 like the GPU (the
 // increments are exact, so removal/completion counts match bit for bit).
+//
+// Also restated: the coupled fixed-population solver
+// (SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu:648-1015: unit weights, its
+// complementary tension with the neighbour's own support, no clamp, no state
+// changes) and the colour / energy output (SPH2S_FINAL_TWO_SCALE/Solver.cu:
+// 206-213, 378-387, 897-907, 1050-1070).  Defined here, replacing the
+// reference's render-pass surface flag (SSFRenderer.cu:196-218) and its
+// commented-out split marking (Solver.cu:1077-1082): the surface trigger
+// splits a normal LOW particle with rho < surface_density and merges a group
+// whose 8 members are fully blended in and all have rho >= surface_density,
+// both on the densities of the current step.
 // ============================================================================
 #include <cmath>
 #include <cstdint>
@@ -69,6 +80,9 @@ struct OConfig2 {
     OGrid grid[2];
     int32_t refine_axis;
     float refine_lo, refine_hi;
+    int32_t mode;           // 0 blended, 1 coupled
+    int32_t split_trigger;  // 0 slab, 1 surface
+    float surface_density;
 };
 
 struct TPop {
@@ -139,7 +153,7 @@ void sort_pop(const OGrid& g, const TPop& in, SortedPop& out) {
 }
 
 struct Fields {
-    std::vector<double> rho, p, acc;
+    std::vector<double> rho, p, acc, colour, dist_cm;
     std::vector<uint32_t> nbr_same, nbr_compl, nbr_bnd;
 };
 
@@ -158,6 +172,7 @@ void ts_density(const OConfig2& C, int r, const SortedPop* P, Fields& F) {
     const float Tr = thresh_sq(hr), T0 = thresh_sq(h0);
     const Kern Kr(hr), K0(C.effective_radius[LOW]), K1(C.effective_radius[HIGH]);
     const double mr = C.fluid_particle_mass[r], mc = C.fluid_particle_mass[c];
+    const bool coupled = C.mode == 1;
     F.rho.assign(n, 0.0);
     F.p.assign(n, 0.0);
     F.nbr_same.assign(n, 0);
@@ -170,7 +185,7 @@ void ts_density(const OConfig2& C, int r, const SortedPop* P, Fields& F) {
         uint32_t ns = 0, nc = 0;
         for_stencil(C.grid[r], S.set.cells, xi, hr, [&](uint32_t j) {
             if (r2_f32(xi, &S.xf[3 * j]) < Tr) {
-                s += S.p.lam[j] * Kr.W(dist(xd, &S.p.x[3 * j], d));
+                s += (coupled ? 1.0 : S.p.lam[j]) * Kr.W(dist(xd, &S.p.x[3 * j], d));
                 ++ns;
             }
         });
@@ -178,7 +193,7 @@ void ts_density(const OConfig2& C, int r, const SortedPop* P, Fields& F) {
             if (r2_f32(xi, &O.xf[3 * j]) < T0) {
                 const double rr = dist(xd, &O.p.x[3 * j], d);
                 const double w1 = rr < K1.h ? K1.W(rr) : 0.0;
-                sc += O.p.lam[j] * 0.5 * (K0.W(rr) + w1);
+                sc += (coupled ? 1.0 : O.p.lam[j]) * 0.5 * (K0.W(rr) + w1);
                 ++nc;
             }
         });
@@ -202,8 +217,12 @@ void ts_accel(const OConfig2& C, int r, const SortedPop* P, const Fields* F, con
     const double mr = C.fluid_particle_mass[r], mc = C.fluid_particle_mass[c];
     const double mb = C.boundary_particle_mass, m0 = C.fluid_particle_mass[LOW];
     const double mu = C.viscosity, sigma = C.tension_coefficient;
+    const bool coupled = C.mode == 1;
+    const double hmc = 0.8673250705840776;  // Mexican hat 2 / (sqrt(3) pi^(1/4))
     out.acc.assign(3 * n, 0.0);
     out.nbr_bnd.assign(n, 0);
+    out.colour.assign(n, 0.0);
+    out.dist_cm.assign(n, 0.0);
     const std::vector<double>& rho = F[r].rho;
     const std::vector<double>& pr = F[r].p;
 #pragma omp parallel for schedule(dynamic, 256)
@@ -213,11 +232,22 @@ void ts_accel(const OConfig2& C, int r, const SortedPop* P, const Fields* F, con
         const double* vi = &S.p.v[3 * i];
         const double ri = rho[i], pi = pr[i];
         double f[3] = {0, 0, 0}, b[3] = {0, 0, 0}, d[3];
+        const double psi0 = -3.0 * hmc;
+        double psum = psi0, cw[3] = {vi[0] * psi0, vi[1] * psi0, vi[2] * psi0};
+        double cs[3] = {xd[0], xd[1], xd[2]}, ccnt = 1.0;
         for_stencil(C.grid[r], S.set.cells, xi, hr, [&](uint32_t j) {
             const float r2 = r2_f32(xi, &S.xf[3 * j]);
             if (r2 != 0.0f && r2 < Tr) {
                 const double rr = dist(xd, &S.p.x[3 * j], d);
-                const double lj = S.p.lam[j];
+                const double q2 = rr * rr / ((double)hr * (double)hr);
+                const double psi = hmc * (q2 - 3.0) * std::exp(-0.5 * q2);
+                psum += psi;
+                for (int a = 0; a < 3; ++a) {
+                    cw[a] += S.p.v[3 * j + a] * psi;
+                    cs[a] += S.p.x[3 * j + a];
+                }
+                ccnt += 1.0;
+                const double lj = coupled ? 1.0 : S.p.lam[j];
                 const double coeffP = -ri * mr * (pi / (ri * ri) + pr[j] / (rho[j] * rho[j]));
                 const double gw = Kr.gradW_factor(rr);
                 const double coeffV = mu * mr / rho[j] * Kr.lapl(rr);
@@ -233,14 +263,16 @@ void ts_accel(const OConfig2& C, int r, const SortedPop* P, const Fields* F, con
             const float r2 = r2_f32(xi, &O.xf[3 * j]);
             if (r2 != 0.0f && r2 < T0) {
                 const double rr = dist(xd, &O.p.x[3 * j], d);
-                const double lj = O.p.lam[j];
+                const double lj = coupled ? 1.0 : O.p.lam[j];
                 const double coeffP = -ri * mc * (pi / (ri * ri) + p_c[j] / (rho_c[j] * rho_c[j]));
                 const double g1 = rr <= K1.h ? K1.gradW_factor(rr) : 0.0;
                 const double gw = 0.5 * (K0.gradW_factor(rr) + g1);
                 const double l1 = rr < K1.h ? K1.lapl(rr) : 0.0;
                 const double coeffV = mu * mc / rho_c[j] * 0.5 * (K0.lapl(rr) + l1);
                 const double w1 = rr < K1.h ? K1.W(rr) : 0.0;
-                const double coeffT = -0.5 * (K0.W(rr) + w1) * mc * sigma;
+                // coupled: Poly6 of the neighbour's own support (COUPLED/Solver.cu:448-460)
+                const double wt = !coupled ? 0.5 * (K0.W(rr) + w1) : (c == LOW ? K0.W(rr) : w1);
+                const double coeffT = -wt * mc * sigma;
                 for (int a = 0; a < 3; ++a)
                     f[a] += lj * (coeffP * gw * d[a] + coeffV * (O.p.v[3 * j + a] - vi[a]) +
                                   coeffT * d[a]);
@@ -259,6 +291,15 @@ void ts_accel(const OConfig2& C, int r, const SortedPop* P, const Fields* F, con
         out.acc[3 * i + 1] = f[1] / ri - 9.81 + b[1];
         out.acc[3 * i + 2] = f[2] / ri + b[2];
         out.nbr_bnd[i] = bc;
+        double e2 = 0.0, ene = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            const double da = xd[a] - cs[a] / ccnt;
+            e2 += da * da;
+            ene += cw[a] * cw[a];
+        }
+        ene = std::min(ene / (psum * psum * (double)hr), 300.0);
+        out.dist_cm[i] = std::sqrt(e2);
+        out.colour[i] = out.dist_cm[i] < 0.0025 ? 0.3 : ene / 300.0;
     }
 }
 
@@ -289,25 +330,31 @@ void ts_step(TSState& S, double dt, SortedPop* keep_sorted, Fields* keep_fields)
     sort_pop(C.grid[LOW], S.pop[LOW], P[LOW]);
     sort_pop(C.grid[HIGH], S.pop[HIGH], P[HIGH]);
 
-    // groups at the start of the step (fixed-point centroid along the slab axis)
-    const bool refine = C.refine_axis >= 0 && C.refine_axis < 3;
+    Fields F[2], A[2];
+    ts_density(C, HIGH, P, F[HIGH]);
+    ts_density(C, LOW, P, F[LOW]);
+
+    // groups: slab trigger on the start-of-step centroid (fixed point along the
+    // axis), surface trigger on this step's member densities
+    const bool coupled = C.mode == 1;
+    const bool surface = !coupled && C.split_trigger == 1;
+    const bool refine = !coupled && !surface && C.refine_axis >= 0 && C.refine_axis < 3;
+    const float surf_rho = C.surface_density;
     const int ax = refine ? C.refine_axis : 0;
     std::vector<int64_t> gsum(S.group_base, 0);
-    std::vector<uint32_t> gready(S.group_base, 0);
+    std::vector<uint32_t> gready(S.group_base, 0), gsurf(S.group_base, 0);
     for (size_t k = 0; k < P[HIGH].p.size(); ++k) {
         const uint32_t g = P[HIGH].p.group[k];
         if (g == kNoGroup || g >= S.group_base) continue;
         gsum[g] += fixed40(P[HIGH].xf[3 * k + ax]);
         gready[g] += P[HIGH].p.state[k] == 4 ? 1u : 0u;
+        gsurf[g] += F[HIGH].rho[k] < (double)surf_rho ? 1u : 0u;
     }
     const int64_t L = fixed43(C.refine_lo), H = fixed43(C.refine_hi);
     std::vector<uint8_t> merge(S.group_base, 0);
     for (uint32_t g = 0; g < S.group_base; ++g)
-        merge[g] = refine && gready[g] == 8 && !(L < gsum[g] && gsum[g] < H);
-
-    Fields F[2], A[2];
-    ts_density(C, HIGH, P, F[HIGH]);
-    ts_density(C, LOW, P, F[LOW]);
+        merge[g] = gready[g] == 8 &&
+                   ((refine && !(L < gsum[g] && gsum[g] < H)) || (surface && gsurf[g] == 0));
     ts_accel(C, HIGH, P, F, S.B, A[HIGH]);
     ts_accel(C, LOW, P, F, S.B, A[LOW]);
 
@@ -330,7 +377,7 @@ void ts_step(TSState& S, double dt, SortedPop* keep_sorted, Fields* keep_fields)
             double v[3], x[3];
             for (int a = 0; a < 3; ++a) v[a] = Q.p.v[3 * i + a] + dt * A[r].acc[3 * i + a];
             const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-            if (nv > vmax && nv > 0.0)
+            if (!coupled && nv > vmax && nv > 0.0)
                 for (int a = 0; a < 3; ++a) v[a] *= vmax / nv;
             for (int a = 0; a < 3; ++a) x[a] = Q.p.x[3 * i + a] + dt * v[a];
             int32_t state = Q.p.state[i];
@@ -338,6 +385,12 @@ void ts_step(TSState& S, double dt, SortedPop* keep_sorted, Fields* keep_fields)
             const float xa = Q.xf[3 * i + ax];
             if (r == LOW && refine && (state & 3) == 0 && C.refine_lo < xa && xa < C.refine_hi)
                 state = (state & 4) | 3;
+            if (r == LOW && surface && (state & 3) == 0 && F[LOW].rho[i] < (double)surf_rho)
+                state = (state & 4) | 3;
+            if (coupled) {  // fixed populations: no blend, no state changes
+                next[r].push(x, v, Q.p.lam[i], state, group, Q.p.ids[i]);
+                continue;
+            }
             float lam = Q.p.lam[i] + cblend[state & 3] * C.blend_increment;
             if (lam <= 0.0f && (state & 3) == 1) {
                 st.removed[r]++;
@@ -401,6 +454,8 @@ void ts_step(TSState& S, double dt, SortedPop* keep_sorted, Fields* keep_fields)
             keep_fields[r] = F[r];
             keep_fields[r].acc = A[r].acc;
             keep_fields[r].nbr_bnd = A[r].nbr_bnd;
+            keep_fields[r].colour = A[r].colour;
+            keep_fields[r].dist_cm = A[r].dist_cm;
         }
     }
     S.pop[LOW] = std::move(next[LOW]);
@@ -459,7 +514,8 @@ void or_ts_advance(void* h, double dt, int steps) {
 // sorted persistent ids.  Arrays per population r sized by the pre-step count.
 void or_ts_step_fields(void* h, double dt, double* const* rho, double* const* acc,
                        uint32_t* const* nbr_same, uint32_t* const* nbr_compl,
-                       uint32_t* const* nbr_bnd, uint32_t* const* ids_sorted) {
+                       uint32_t* const* nbr_bnd, uint32_t* const* ids_sorted,
+                       double* const* colour, double* const* dist_cm) {
     TSState* S = (TSState*)h;
     SortedPop P[2];
     Fields F[2];
@@ -472,6 +528,8 @@ void or_ts_step_fields(void* h, double dt, double* const* rho, double* const* ac
         if (nbr_compl && nbr_compl[r]) std::memcpy(nbr_compl[r], F[r].nbr_compl.data(), n * 4);
         if (nbr_bnd && nbr_bnd[r]) std::memcpy(nbr_bnd[r], F[r].nbr_bnd.data(), n * 4);
         if (ids_sorted && ids_sorted[r]) std::memcpy(ids_sorted[r], P[r].p.ids.data(), n * 4);
+        if (colour && colour[r]) std::memcpy(colour[r], F[r].colour.data(), n * 8);
+        if (dist_cm && dist_cm[r]) std::memcpy(dist_cm[r], F[r].dist_cm.data(), n * 8);
     }
 }
 

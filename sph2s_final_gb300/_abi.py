@@ -65,6 +65,9 @@ class sph_config2(C.Structure):
         ("refine_axis", C.c_int32),
         ("refine_lo", C.c_float),
         ("refine_hi", C.c_float),
+        ("mode", C.c_int32),
+        ("split_trigger", C.c_int32),
+        ("surface_density", C.c_float),
     ]
 
 
@@ -123,6 +126,8 @@ SIGNATURES = {
     "sph2_get_state": (C.c_int, [_vp, C.c_int32, _f, _f, _f, C.POINTER(C.c_int32), _u, _u]),
     "sph2_debug_step_fields": (C.c_int, [_vp, C.c_int32, _u, _f, _f, _u, _u, _u]),
     "sph2_destroy": (C.c_int, [_vp]),
+    "sph2_set_color_output": (C.c_int, [_vp, C.c_int32]),
+    "sph2_get_colors": (C.c_int, [_vp, C.c_int32, _f, _u, _u]),
     "sphb_create": (C.c_int, [C.POINTER(sph_scene_desc), C.c_uint32, C.POINTER(_vp)]),
     "sphb_advance": (C.c_int, [_vp, C.c_float, C.c_int32]),
     "sphb_sync": (C.c_int, [_vp]),

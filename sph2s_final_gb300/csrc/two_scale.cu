@@ -79,6 +79,9 @@ struct sph_solver2 {
     uint32_t stats[6] = {0, 0, 0, 0, 0, 0};
     uint32_t next_id[2] = {0, 0};  // persistent id of the next particle created (LOW, HIGH)
     uint64_t step = 0;             // steps advanced since creation
+    float* colour[2] = {nullptr, nullptr};  // colour output of the last step
+    bool colour_on = false;
+    uint32_t colour_n[2] = {0, 0};          // particles of that step per population
     std::vector<void*> owned;
 };
 
@@ -102,6 +105,12 @@ int make_ts_params(const sph_config2& c, TSParams* out) {
             return fail(SPH_E_INVALID, "sph_config2: radii and masses must be positive");
     }
     if (c.refine_axis > 2) return fail(SPH_E_INVALID, "sph_config2: refine_axis must be -1..2");
+    if (c.mode != SPH2_MODE_BLENDED && c.mode != SPH2_MODE_COUPLED)
+        return fail(SPH_E_INVALID, "sph_config2: unknown mode");
+    if (c.split_trigger != SPH2_SPLIT_SLAB && c.split_trigger != SPH2_SPLIT_SURFACE)
+        return fail(SPH_E_INVALID, "sph_config2: unknown split trigger");
+    if (c.split_trigger == SPH2_SPLIT_SURFACE && !(c.surface_density > 0.0f))
+        return fail(SPH_E_INVALID, "sph_config2: surface_density must be positive");
     const double pi = 3.14159265358979323846;
     TSParams P;
     for (int r = 0; r < 2; ++r) {
@@ -123,7 +132,10 @@ int make_ts_params(const sph_config2& c, TSParams* out) {
     P.two_over_h0 = (float)(2.0 / (double)c.effective_radius[0]);
     P.gravity = -9.81f;
     P.blend_inc = c.blend_increment;
-    P.axis = c.refine_axis;
+    P.coupled = c.mode == SPH2_MODE_COUPLED ? 1 : 0;
+    P.surface = (!P.coupled && c.split_trigger == SPH2_SPLIT_SURFACE) ? 1 : 0;
+    P.surf_rho = c.surface_density;
+    P.axis = (P.coupled || P.surface) ? -1 : c.refine_axis;
     P.lo = c.refine_lo;
     P.hi = c.refine_hi;
     P.lo43 = std::llrint((double)c.refine_lo * 8796093022208.0);
@@ -151,8 +163,9 @@ int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, std::vector<void*>& o) {
     return SPH_OK;
 }
 
-TSOut outputs(Pop& p, float* acc, uint32_t* nbr_bnd) {
+TSOut outputs(Pop& p, float* acc, uint32_t* nbr_bnd, float* colour = nullptr) {
     TSOut o;
+    o.colour = colour;
     o.ipos = p.ipos;
     o.ivel = p.ivel;
     o.istt = p.istt;
@@ -180,11 +193,12 @@ void ts_neighborhood(sph_solver2* s, int r) {
     if (r == 1)
         ts_gather_kernel<true><<<blocks_for(p.n), 256, 0, st>>>(
             s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
-            p.sstt, p.sgrp, p.cells, s->err, s->P.axis, s->group_base, s->gsum, s->gready);
+            p.sstt, p.sgrp, p.cells, s->err, s->P.axis, s->P.surface, s->group_base, s->gsum,
+            s->gready);
     else
         ts_gather_kernel<false><<<blocks_for(p.n), 256, 0, st>>>(
             s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
-            p.sstt, p.sgrp, p.cells, s->err, -1, 0, nullptr, nullptr);
+            p.sstt, p.sgrp, p.cells, s->err, -1, 0, 0, nullptr, nullptr);
 }
 
 // Everything up to and including the force/integrate pass; DEBUG variants
@@ -201,50 +215,55 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
     cudaMemsetAsync(s->ctl + kCtlFadedL, 0, 8, st);
     ts_neighborhood(s, 1);
     ts_neighborhood(s, 0);
-    if (gb && s->P.axis >= 0)
-        ts_group_decide_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gsum, s->gready, gb, s->P.lo43,
-                                                               s->P.hi43, s->gmerge);
-    else if (gb)
-        cudaMemsetAsync(s->gmerge, 0, 4 * (size_t)gb, st);
     Pop &L = s->pop[0], &H = s->pop[1];
     if (H.n) {
         if (debug && dbg_pop == 1)
             ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
-                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, dnb_same, dnb_compl);
+                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, dnb_same, dnb_compl,
+                H.sgrp, gb, s->gsum);
         else
             ts_density_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
-                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, nullptr, nullptr);
+                H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, nullptr, nullptr,
+                H.sgrp, gb, s->gsum);
     }
     if (L.n) {
         if (debug && dbg_pop == 0)
             ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
-                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl);
+                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl,
+                L.sgrp, gb, s->gsum);
         else
             ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
-                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr);
+                L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr,
+                L.sgrp, gb, s->gsum);
     }
+    // merge decisions (slab: start-of-step centroids; surface: this step's densities)
+    if (gb && (s->P.axis >= 0 || s->P.surface))
+        ts_group_decide_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gsum, s->gready, gb, s->P.lo43,
+                                                               s->P.hi43, s->P.surface, s->gmerge);
+    else if (gb)
+        cudaMemsetAsync(s->gmerge, 0, 4 * (size_t)gb, st);
     const uint32_t* gm = gb ? s->gmerge : nullptr;
     if (H.n) {
-        TSOut o = outputs(H, dacc, dnb_bnd);
+        TSOut o = outputs(H, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[1] : nullptr);
         if (debug && dbg_pop == 1)
             ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, o);
         else
             ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, o);
     }
     if (L.n) {
-        TSOut o = outputs(L, dacc, dnb_bnd);
+        TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
             ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, o);
         else
             ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, o);
     }
 }
 
@@ -302,6 +321,8 @@ int ts_step(sph_solver2* s, float dt) {
     s->stats[3] = H.n - c[kCtlSurvH];
     s->stats[4] = c[kCtlFadedL];
     s->stats[5] = c[kCtlFadedH];
+    s->colour_n[0] = L.n;
+    s->colour_n[1] = H.n;
     H.n = c[kCtlNextH];
     L.n = c[kCtlNextL];
     s->group_base = c[kCtlGroupBase];
@@ -616,6 +637,38 @@ int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sor
 }
 
 int sph2_destroy(sph_solver2* s) { return free_solver2(s); }
+
+int sph2_set_color_output(sph_solver2* s, int32_t on) {
+    if (!s) return fail(SPH_E_INVALID, "sph2_set_color_output: NULL handle");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (on && !s->colour[0]) {
+        for (int r = 0; r < 2; ++r) {
+            int rc = dalloc(&s->colour[r], s->pop[r].cap, s->owned);
+            if (rc != SPH_OK) return rc;
+        }
+    }
+    s->colour_on = on != 0;
+    s->colour_n[0] = s->colour_n[1] = 0;
+    return SPH_OK;
+}
+
+int sph2_get_colors(sph_solver2* s, int32_t population, float* colour, uint32_t* ids_sorted,
+                    uint32_t* count) {
+    if (!s || population < 0 || population > 1)
+        return fail(SPH_E_INVALID, "sph2_get_colors: bad handle or population");
+    const uint32_t n = s->colour_on ? s->colour_n[population] : 0u;
+    if (count) *count = n;
+    if (!colour && !ids_sorted) return SPH_OK;
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (n && colour)
+        SPH_CUDA(cudaMemcpy(colour, s->colour[population], 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (n && ids_sorted) {
+        std::vector<float4> sv(n);
+        SPH_CUDA(cudaMemcpy(sv.data(), s->pop[population].svel, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+        for (uint32_t k = 0; k < n; ++k) std::memcpy(&ids_sorted[k], &sv[k].w, 4);
+    }
+    return SPH_OK;
+}
 
 // ---- state I/O (formats in state_format.h) ---------------------------------
 // Two-scale state body:

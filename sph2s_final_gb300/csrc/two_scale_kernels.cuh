@@ -28,10 +28,17 @@ struct TSParams {
     float two_over_h0;
     float gravity;
     float blend_inc;
-    int axis;                 // refinement slab axis, -1 = no split/merge
+    int axis;                 // refinement slab axis, -1 = no slab split/merge
     float lo, hi;
     long long lo43, hi43;     // slab bounds in the group-centroid fixed point (x 2^43)
+    int coupled;              // fixed populations: unit weights, no clamp, no state changes
+    int surface;              // surface trigger: split / merge by rho < surf_rho
+    float surf_rho;
 };
+
+// Mexican hat wavelet of the colour output (evaluateMexicanHat3D,
+// SPH2S_FINAL_TWO_SCALE/Solver.cu:206-213): c (q2 - 3) exp(-q2 / 2), q2 = |x/h|^2.
+constexpr float kMexicanHatC = 0.8673250705840776f;  // 2 / (sqrt(3) pi^(1/4))
 
 // Per-step control words on the device (written by ts_totals_kernel).
 enum TSCtl {
@@ -62,8 +69,8 @@ __global__ void __launch_bounds__(256) ts_gather_kernel(
     GridParams g, const float4* __restrict__ pos, const float4* __restrict__ vel,
     const int32_t* __restrict__ stt, const uint32_t* __restrict__ grp, float4* __restrict__ spos,
     float4* __restrict__ svel, int32_t* __restrict__ sstt, uint32_t* __restrict__ sgrp,
-    uint2* __restrict__ cells, uint32_t* __restrict__ err, int axis, uint32_t group_base,
-    unsigned long long* __restrict__ gsum, uint32_t* __restrict__ gready) {
+    uint2* __restrict__ cells, uint32_t* __restrict__ err, int axis, int surface,
+    uint32_t group_base, unsigned long long* __restrict__ gsum, uint32_t* __restrict__ gready) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t q = perm[i];
@@ -78,9 +85,11 @@ __global__ void __launch_bounds__(256) ts_gather_kernel(
     const uint32_t gid = grp[q];
     sstt[i] = s;
     sgrp[i] = gid;
-    if (HIGH_POP && axis >= 0 && gid != kNoGroup && gid < group_base) {
-        const float xa = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
-        atomicAdd(&gsum[gid], (unsigned long long)fixed40(xa));
+    if (HIGH_POP && (axis >= 0 || surface) && gid != kNoGroup && gid < group_base) {
+        if (axis >= 0) {
+            const float xa = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+            atomicAdd(&gsum[gid], (unsigned long long)fixed40(xa));
+        }
         if (s == 4) atomicAdd(&gready[gid], 1u);
     }
     const uint32_t key = keys_sorted[i];
@@ -100,14 +109,18 @@ __global__ void __launch_bounds__(256) ts_gather_kernel(
     if (i == n - 1) cw[2 * c + 1] = n;
 }
 
-// merge[g] = all 8 members fully blended in and the centroid outside the slab.
+// merge[g] = all 8 members fully blended in and, for the slab trigger, the
+// centroid outside the slab; for the surface trigger, no member below the
+// surface density (gsum then counts those members).
 static __global__ void __launch_bounds__(256) ts_group_decide_kernel(
     const unsigned long long* __restrict__ gsum, const uint32_t* __restrict__ gready,
-    uint32_t group_base, long long lo43, long long hi43, uint32_t* __restrict__ gmerge) {
+    uint32_t group_base, long long lo43, long long hi43, int surface,
+    uint32_t* __restrict__ gmerge) {
     uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     if (gi >= group_base) return;
     const long long s = (long long)gsum[gi];
-    gmerge[gi] = (gready[gi] == 8u && !(lo43 < s && s < hi43)) ? 1u : 0u;
+    const bool away = surface ? s == 0 : !(lo43 < s && s < hi43);
+    gmerge[gi] = (gready[gi] == 8u && away) ? 1u : 0u;
 }
 
 // Density of population r: same population weighted by lambda_j, plus the
@@ -118,7 +131,8 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
     const float4* __restrict__ spos_r, const uint2* __restrict__ cells_r, uint32_t n_r,
     const float4* __restrict__ spos_c, const uint2* __restrict__ cells_c, uint32_t n_c,
     TSParams P, float* __restrict__ rho, float2* __restrict__ aux, uint32_t* __restrict__ nbr_same,
-    uint32_t* __restrict__ nbr_compl) {
+    uint32_t* __restrict__ nbr_compl, const uint32_t* __restrict__ sgrp_r, uint32_t group_base,
+    unsigned long long* __restrict__ gsurf) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -139,7 +153,7 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                         const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
                         if (r2 < P.T[R]) {
                             const float a = P.h2[R] - r2;
-                            s = fmaf(xj.w, a * a * a, s);
+                            s = fmaf(P.coupled ? 1.0f : xj.w, a * a * a, s);
                             if (DEBUG) ++ns;
                         }
                     }
@@ -162,7 +176,7 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                             const float a0 = P.h2[0] - r2, a1 = P.h2[1] - r2;
                             float w = P.poly6[0] * a0 * a0 * a0;
                             if (r2 < P.T[1]) w += P.poly6[1] * a1 * a1 * a1;
-                            sc = fmaf(xj.w, 0.5f * w, sc);
+                            sc = fmaf(P.coupled ? 1.0f : xj.w, 0.5f * w, sc);
                             if (DEBUG) ++nc;
                         }
                     }
@@ -178,6 +192,10 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
         nbr_same[i] = ns;
         nbr_compl[i] = nc;
     }
+    if (R == 1 && P.surface && rh < P.surf_rho) {  // members of a group at the surface
+        const uint32_t gid = sgrp_r[i];
+        if (gid != kNoGroup && gid < group_base) atomicAdd(&gsurf[gid], 1ull);
+    }
 }
 
 struct TSOut {
@@ -189,6 +207,7 @@ struct TSOut {
     uint32_t* split;  // LOW only: emits 8 children
     float* acc;       // DEBUG: accelerations (3 per particle)
     uint32_t* nbr_bnd;
+    float* colour;    // colour / energy output per particle of the step's sorted order, or null
 };
 
 // Accelerations (SPH2S_FINAL_TWO_SCALE/Solver.cu:847-1048) and integration
@@ -202,7 +221,8 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     const float2* __restrict__ aux_c, const uint2* __restrict__ cells_c, uint32_t n_c,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells, uint32_t nb, TSParams P,
     float dt, const uint32_t* __restrict__ gmerge, uint32_t n_groups,
-    unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl, TSOut out) {
+    unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl,
+    const float* __restrict__ rho_r, TSOut out) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -210,6 +230,13 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     const float4 vi = svel_r[i];
     const float2 ai = aux_r[i];
     float fx = 0.f, fy = 0.f, fz = 0.f, wx = 0.f, wy = 0.f, wz = 0.f;
+    // colour output (Solver.cu:897-907, 378-387, 1050-1070): Mexican-hat velocity
+    // wavelet and mass centre over the same population, self included
+    const bool colour = out.colour != nullptr;
+    const float psi0 = -3.0f * kMexicanHatC;
+    float psum = psi0, cwx = vi.x * psi0, cwy = vi.y * psi0, cwz = vi.z * psi0;
+    float csx = xi.x, csy = xi.y, csz = xi.z, ccnt = 1.0f;
+    const float inv_h2 = 1.0f / P.h2[R];
     {
         const float tco = P.sigma * P.mass[R] * P.poly6[R] * ai.y;
         const float pco = P.mass[R] * P.spiky[R];
@@ -230,14 +257,27 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
                             const float rs = rsqrtf(r2);
                             const float hr = P.h[R] - r2 * rs;
                             const float a = P.h2[R] - r2;
-                            const float sc = xj.w * (pco * (ai.x + aj.x) * hr * hr * rs - tco * a * a * a);
+                            const float lj = P.coupled ? 1.0f : xj.w;
+                            const float sc = lj * (pco * (ai.x + aj.x) * hr * hr * rs - tco * a * a * a);
                             fx = fmaf(sc, dx, fx);
                             fy = fmaf(sc, dy, fy);
                             fz = fmaf(sc, dz, fz);
-                            const float vc = xj.w * aj.y * hr * P.spiky[R] * P.mass[R];
+                            const float vc = lj * aj.y * hr * P.spiky[R] * P.mass[R];
                             wx = fmaf(vc, vj.x - vi.x, wx);
                             wy = fmaf(vc, vj.y - vi.y, wy);
                             wz = fmaf(vc, vj.z - vi.z, wz);
+                            if (colour) {
+                                const float q2 = r2 * inv_h2;
+                                const float psi = kMexicanHatC * (q2 - 3.0f) * expf(-0.5f * q2);
+                                psum += psi;
+                                cwx = fmaf(vj.x, psi, cwx);
+                                cwy = fmaf(vj.y, psi, cwy);
+                                cwz = fmaf(vj.z, psi, cwz);
+                                csx += xj.x;
+                                csy += xj.y;
+                                csz += xj.z;
+                                ccnt += 1.0f;
+                            }
                         }
                     }
                 }
@@ -271,12 +311,18 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
                                 l += P.spiky[1] * h1r;
                                 w += P.poly6[1] * a1 * a1 * a1;
                             }
-                            const float sc = xj.w * (P.mass[C] * (ai.x + aj.x) * 0.5f * g * rs -
-                                                     P.sigma * P.mass[C] * 0.5f * w * ai.y);
+                            // coupled: the neighbour support's Poly6 for tension
+                            // (SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu:448-460)
+                            const float wt = !P.coupled ? 0.5f * w
+                                                        : (C == 0 ? P.poly6[0] * a0 * a0 * a0
+                                                                  : (in1 ? P.poly6[1] * a1 * a1 * a1 : 0.0f));
+                            const float lj = P.coupled ? 1.0f : xj.w;
+                            const float sc = lj * (P.mass[C] * (ai.x + aj.x) * 0.5f * g * rs -
+                                                   P.sigma * P.mass[C] * wt * ai.y);
                             fx = fmaf(sc, dx, fx);
                             fy = fmaf(sc, dy, fy);
                             fz = fmaf(sc, dz, fz);
-                            const float vc = xj.w * P.mass[C] * aj.y * 0.5f * l;
+                            const float vc = lj * P.mass[C] * aj.y * 0.5f * l;
                             wx = fmaf(vc, vj.x - vi.x, wx);
                             wy = fmaf(vc, vj.y - vi.y, wy);
                             wz = fmaf(vc, vj.z - vi.z, wz);
@@ -323,11 +369,20 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         out.acc[3 * i + 2] = azz;
         out.nbr_bnd[i] = bcnt;
     }
-    // integrate with the velocity clamp |v| <= 0.8 h_r / dt (Solver.cu:1207-1227)
+    if (colour) {  // Solver.cu:1050-1070
+        const float inv_c = 1.0f / ccnt;
+        const float ex = xi.x - csx * inv_c, ey = xi.y - csy * inv_c, ez = xi.z - csz * inv_c;
+        const float dist_cm = sqrtf(ex * ex + ey * ey + ez * ez);
+        float ene = (cwx * cwx + cwy * cwy + cwz * cwz) / (psum * psum * P.h[R]);
+        ene = fminf(ene, 300.0f);
+        out.colour[i] = dist_cm < 0.0025f ? 0.3f : ene / 300.0f;
+    }
+    // integrate with the velocity clamp |v| <= 0.8 h_r / dt (Solver.cu:1207-1227);
+    // the coupled solver integrates without it (SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu:930-970)
     float nvx = fmaf(dt, axx, vi.x), nvy = fmaf(dt, ayy, vi.y), nvz = fmaf(dt, azz, vi.z);
     const float norm = sqrtf(nvx * nvx + nvy * nvy + nvz * nvz);
     const float vmax = 0.8f * P.h[R] / dt;
-    if (norm > vmax) {
+    if (!P.coupled && norm > vmax) {
         const float sc = vmax / norm;
         nvx *= sc;
         nvy *= sc;
@@ -341,7 +396,8 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         const float xa = P.axis == 0 ? xi.x : (P.axis == 1 ? xi.y : xi.z);
         if (P.lo < xa && xa < P.hi) state = (state & 4) | 3;
     }
-    const int sb = state & 3;
+    if (R == 0 && P.surface && (state & 3) == 0 && rho_r[i] < P.surf_rho) state = (state & 4) | 3;
+    const int sb = P.coupled ? 0 : (state & 3);
     const float cb = sb == 1 ? -1.0f : (sb == 2 ? 1.0f : 0.0f);
     float lam = __fadd_rn(xi.w, __fmul_rn(cb, P.blend_inc));
     uint32_t keep = 1u, split = 0u;
@@ -351,7 +407,7 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         lam = 1.0f;
         atomicAdd(&ctl[R == 0 ? kCtlFadedL : kCtlFadedH], 1u);
     }
-    if (keep && R == 0 && (state & 3) == 3) {
+    if (keep && R == 0 && !P.coupled && (state & 3) == 3) {
         split = 1u;
         state = 1;
     }

@@ -113,6 +113,20 @@ class Solver2:
                                            uptr(r["nbr_compl"]), uptr(r["nbr_boundary"])))
         return r
 
+    def set_color_output(self, on: bool = True) -> None:
+        """Colour / energy output of the force pass (dColorValues), off by default."""
+        check(lib().sph2_set_color_output(self._h, 1 if on else 0))
+
+    def colors(self, population: int):
+        """Last step's colour values of one population in that step's sorted
+        order, with the persistent ids."""
+        n = C.c_uint32()
+        check(lib().sph2_get_colors(self._h, population, None, None, C.byref(n)))
+        col = np.empty(n.value, np.float32)
+        ids = np.empty(n.value, np.uint32)
+        check(lib().sph2_get_colors(self._h, population, fptr(col), uptr(ids), C.byref(n)))
+        return col, ids
+
     # ---- headless state I/O (state_io.py describes the formats) ----
     @property
     def step_count(self) -> int:
