@@ -437,15 +437,17 @@ def run_ours(args):
     solver.close()
 
     # end to end through the public API: create from host arrays, then per step
-    # advance + positions read back into pinned host memory.
-    pinned = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-    from sph2s_final_gb300 import _abi
+    # advance + positions read back into pinned host memory (sph_get_positions_async:
+    # the copy of step k overlaps step k+1; two pinned buffers alternate), and a
+    # final sync that waits for the last copy.
+    pinned = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     barrier()
     t0 = time.perf_counter()
     s2 = Solver(sc.fluid, sc.boundary, sc.config)
-    for _ in range(args.steps):
+    for k in range(args.steps):
         s2.advance(sc.dt, 1)
-        _abi.check(_abi.lib().sph_get_positions(s2._h, _abi.fptr(pinned), _abi.SPH_ORDER_SORTED))
+        s2.positions_async(pinned[k & 1])
+    s2.sync()
     t1 = time.perf_counter()
     s2.close()
     e2e_s = replicas.max_over_ranks(t1 - t0, device="cuda")

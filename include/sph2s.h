@@ -109,6 +109,14 @@ int sph_sync(sph_solver* s);
 int sph_get_positions(sph_solver* s, float* xyz, int32_t order);
 int sph_get_velocities(sph_solver* s, float* xyz, int32_t order);
 int sph_get_densities(sph_solver* s, float* rho, int32_t order);
+/* Enqueues a readback of the current positions (3 floats per particle) into
+ * xyz and returns at once: the positions are packed into one of two device
+ * staging buffers on the handle's stream and copied out on a second stream,
+ * so the copy of step k overlaps the computation of step k+1.  xyz must stay
+ * valid, and should be pinned host memory for the copy to be asynchronous,
+ * until sph_sync; at most two readbacks are in flight (a third waits for the
+ * first). */
+int sph_get_positions_async(sph_solver* s, float* xyz, int32_t order);
 /* Persistent ids in sorted order (ids[k] = input index of the k-th particle). */
 int sph_get_ids(sph_solver* s, uint32_t* ids);
 /* Overwrites the velocities (3 floats per particle) in the given order. */

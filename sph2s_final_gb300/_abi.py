@@ -100,6 +100,7 @@ SIGNATURES = {
     "sph_advance": (C.c_int, [_vp, C.c_float, C.c_int32]),
     "sph_sync": (C.c_int, [_vp]),
     "sph_get_positions": (C.c_int, [_vp, _f, C.c_int32]),
+    "sph_get_positions_async": (C.c_int, [_vp, _f, C.c_int32]),
     "sph_get_velocities": (C.c_int, [_vp, _f, C.c_int32]),
     "sph_get_densities": (C.c_int, [_vp, _f, C.c_int32]),
     "sph_get_ids": (C.c_int, [_vp, _u]),

@@ -30,6 +30,13 @@ int free_solver(sph_solver* s) {
                     s->bnear,   s->pos0, s->xacc, s->xall, s->xnb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
+    for (int b = 0; b < 2; ++b) {
+        if (s->astage[b]) cudaFree(s->astage[b]);
+        if (s->packed[b]) cudaEventDestroy(s->packed[b]);
+        if (s->copied[b]) cudaEventDestroy(s->copied[b]);
+    }
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->err_host) cudaFreeHost(s->err_host);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -308,7 +315,35 @@ int sph_advance(sph_solver* s, float dt, int32_t steps) {
 int sph_sync(sph_solver* s) {
     if (!s) return fail(SPH_E_INVALID, "sph_sync: NULL handle");
     SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->copy_stream) SPH_CUDA(cudaStreamSynchronize(s->copy_stream));
     return check_device_error(s);
+}
+
+int sph_get_positions_async(sph_solver* s, float* xyz, int32_t order) {
+    if (!s || (!xyz && s->n)) return fail(SPH_E_INVALID, "sph_get_positions_async: NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    if (s->n == 0) return SPH_OK;
+    if (!s->copy_stream) {
+        SPH_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            SPH_CUDA(cudaEventCreateWithFlags(&s->packed[b], cudaEventDisableTiming));
+            SPH_CUDA(cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming));
+            SPH_CUDA(cudaMalloc(&s->astage[b], 12 * (size_t)s->n));
+        }
+    }
+    const int b = s->abuf;
+    s->abuf ^= 1;
+    // the last copy out of this staging buffer has drained before it is refilled
+    SPH_CUDA(cudaStreamWaitEvent(s->stream, s->copied[b], 0));
+    pack_xyz_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(s->pos, s->pos, s->n,
+                                                             order == SPH_ORDER_BY_ID, s->astage[b]);
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaEventRecord(s->packed[b], s->stream));
+    SPH_CUDA(cudaStreamWaitEvent(s->copy_stream, s->packed[b], 0));
+    SPH_CUDA(cudaMemcpyAsync(xyz, s->astage[b], 12 * (size_t)s->n, cudaMemcpyDeviceToHost,
+                             s->copy_stream));
+    SPH_CUDA(cudaEventRecord(s->copied[b], s->copy_stream));
+    return SPH_OK;
 }
 
 int sph_get_positions(sph_solver* s, float* xyz, int32_t order) {

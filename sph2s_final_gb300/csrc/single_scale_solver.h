@@ -44,6 +44,11 @@ struct sph_solver {
     float* xacc = nullptr;     // XSPH integrator: accelerations of the step (3 per particle)
     uint32_t* xall = nullptr;  // XSPH integrator: neighbours incl. distance 0, per particle
     uint32_t* xnb = nullptr;   // XSPH integrator: boundary neighbour counts (unused output)
+    // asynchronous position readback: two device staging buffers drained by a copy stream
+    float* astage[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t packed[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    int abuf = 0;
     sph::Rollout* rollout = nullptr;
 };
 

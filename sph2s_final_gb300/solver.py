@@ -235,6 +235,13 @@ class Solver:
     def debug_force_lookback_timeout(self, on: bool) -> None:
         check(lib().sph_debug_force_lookback_timeout(self._h, 1 if on else 0))
 
+    def positions_async(self, out: np.ndarray, order: str = "sorted") -> None:
+        """Enqueues a readback of the positions into `out` (float32 (n, 3), best
+        pinned); valid after sync().  The copy overlaps the next steps."""
+        assert out.dtype == np.float32 and out.shape == (self.num_fluid, 3) and \
+            out.flags.c_contiguous
+        check(lib().sph_get_positions_async(self._h, fptr(out), ORDER[order]))
+
     def set_integrator(self, integrator: str) -> None:
         """"symplectic_euler" (integrateD, the default) or "xsph" (integrateXSPHD,
         Solver.cu:757-853, per-component correction, eps = config.xsph_coeff)."""
