@@ -63,13 +63,13 @@ template <int BS>
 void launch_density(sph_batch* b, int ti) {
     b_density_kernel<BS><<<pgrid(b, b->ntiles[ti]), BS, 0, b->stream>>>(
         b->tiles[ti], b->ntiles[ti], b->recs, b->spos, b->cells, b->N, b->rho, b->aux, b->nbr,
-        b->nbr_count);
+        b->nbr_count, b->xa, b->svel);
 }
 
 template <int BS>
 void launch_force(sph_batch* b, int ti, float dt) {
     b_force_kernel<BS><<<pgrid(b, b->ntiles[ti]), BS, 0, b->stream>>>(
-        b->tiles[ti], b->ntiles[ti], b->recs, b->spos, b->svel, b->aux, b->cells, b->nbr,
+        b->tiles[ti], b->ntiles[ti], b->recs, b->spos, b->xa, b->svel, b->cells, b->nbr,
         b->nbr_count, b->bpos, b->bcells, b->bnear, b->N, b->NB, dt, b->pos, b->vel);
 }
 
@@ -206,6 +206,7 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(dalloc(&b->svel, b->N, b->owned));
     TRY(dalloc(&b->rho, b->N, b->owned));
     TRY(dalloc(&b->aux, b->N, b->owned));
+    TRY(dalloc(&b->xa, b->N, b->owned));
     TRY(dalloc(&b->nbr, (size_t)b->N * (kMaxNbr / 4), b->owned));
     TRY(dalloc(&b->nbr_count, b->N, b->owned));
     for (int k = 0; k < 2; ++k) {

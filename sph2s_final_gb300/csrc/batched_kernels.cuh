@@ -103,21 +103,22 @@ __global__ void __launch_bounds__(BS) b_density_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
     const float4* __restrict__ pos, const uint2* __restrict__ cells, uint32_t n,
     float* __restrict__ rho, float2* __restrict__ aux, uint4* __restrict__ nbr4,
-    uint32_t* __restrict__ nbr_count) {
+    uint32_t* __restrict__ nbr_count, float4* __restrict__ xa, float4* __restrict__ svel) {
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
         const SceneRec& R = recs[tile.x];
         const uint32_t i = tile.y + threadIdx.x;
         if (i >= R.p_off + R.p_n) continue;
         const SimParams P = R.P;
-        density_one<false>(i, pos, cells + R.c_off, n, P, rho, aux, nbr4, nbr_count, nullptr);
+        density_one<false>(i, pos, cells + R.c_off, n, P, rho, aux, nbr4, nbr_count, nullptr, xa,
+                           svel);
     }
 }
 
 template <int BS>
 __global__ void __launch_bounds__(BS) b_force_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
-    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ aux,
+    const float4* __restrict__ pos, const float4* __restrict__ xa, const float4* __restrict__ va,
     const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(BS) b_force_kernel(
         const uint32_t i = tile.y + threadIdx.x;
         if (i >= R.p_off + R.p_n) continue;
         const SimParams P = R.P;
-        force_one<0>(i, pos, vel, aux, cells + R.c_off, nbr4, nbr_count, bpos, bcells + R.c_off,
+        force_one<0>(i, pos, xa, va, cells + R.c_off, nbr4, nbr_count, bpos, bcells + R.c_off,
                      bnear + R.c_off, n, nb, P, dt, pos_out, vel_out, nullptr, nullptr);
     }
 }

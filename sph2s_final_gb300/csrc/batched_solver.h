@@ -25,6 +25,7 @@ struct sph_batch {
     float4 *pos = nullptr, *vel = nullptr, *spos = nullptr, *svel = nullptr;
     float* rho = nullptr;
     float2* aux = nullptr;
+    float4* xa = nullptr;  // force-pass records (x, p/rho^2), written by the density pass
     uint4* nbr = nullptr;
     uint32_t* nbr_count = nullptr;
     uint32_t* keys[2] = {nullptr, nullptr};

@@ -5,7 +5,10 @@
 // [cell(x - h), cell(x + h)] with r < h (self included), p_i = K (rho_i - rho0).
 //
 // Besides rho and the factors the force pass needs from every neighbour
-// (p/rho^2, 1/rho), it emits the force pass's neighbour list: every j with
+// (p/rho^2, 1/rho, in aux), it writes the force pass's per-neighbour records:
+// xa[i] = (x, y, z, p/rho^2) and the w slot of the step's velocity,
+// svel[i].w = 1/rho, so the force pass gathers two 16-byte records per
+// neighbour instead of three loads.  It also emits the neighbour list: every j with
 // 0 < r2 < T, in stencil order.  Lists are stored transposed in groups of
 // four, group g of particle i at nbr4[g * n + i], so the force pass reads 512
 // contiguous bytes per warp instruction; a lane stores a group as soon as it
@@ -36,7 +39,8 @@ __device__ __forceinline__ void density_one(uint32_t i, const float4* __restrict
                                             const SimParams& P, float* __restrict__ rho,
                                             float2* __restrict__ aux, uint4* __restrict__ nbr4,
                                             uint32_t* __restrict__ nbr_count,
-                                            uint32_t* __restrict__ dbg_count) {
+                                            uint32_t* __restrict__ dbg_count,
+                                            float4* __restrict__ xa, float4* __restrict__ svel) {
     uint32_t k = 0, zero = 0;
     uint4 buf = make_uint4(0u, 0u, 0u, 0u);
     float sum = 0.0f;
@@ -77,6 +81,8 @@ __device__ __forceinline__ void density_one(uint32_t i, const float4* __restrict
     const float inv = 1.0f / rh;
     rho[i] = rh;
     aux[i] = make_float2(p * inv * inv, inv);
+    xa[i] = make_float4(xi.x, xi.y, xi.z, p * inv * inv);
+    reinterpret_cast<float*>(svel + i)[3] = inv;
     nbr_count[i] = k;
     if (DEBUG) dbg_count[i] = k + zero;
 }
@@ -85,10 +91,11 @@ template <bool DEBUG>
 __global__ void __launch_bounds__(kDensityThreads) density_kernel(
     const float4* __restrict__ pos, const uint2* __restrict__ cells, uint32_t n, SimParams P,
     float* __restrict__ rho, float2* __restrict__ aux, uint4* __restrict__ nbr4,
-    uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ dbg_count) {
+    uint32_t* __restrict__ nbr_count, uint32_t* __restrict__ dbg_count, float4* __restrict__ xa,
+    float4* __restrict__ svel) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    density_one<DEBUG>(i, pos, cells, n, P, rho, aux, nbr4, nbr_count, dbg_count);
+    density_one<DEBUG>(i, pos, cells, n, P, rho, aux, nbr4, nbr_count, dbg_count, xa, svel);
 }
 
 }  // namespace sph

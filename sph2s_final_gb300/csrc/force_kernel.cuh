@@ -2,7 +2,10 @@
 //
 // computeAccelerationsD + integrateD (SPH2S_FINAL_SINGLE_SCALE/Solver.cu:601-755,
 // with the pair terms of computeAccelerationCell / computeBoundaryForceCell,
-// Solver.cu:231-344).  Fluid neighbours come from the density pass's list.
+// Solver.cu:231-344).  Fluid neighbours come from the density pass's list; each
+// neighbour costs two 16-byte gathers, xa[j] = (x, p/rho^2) and
+// va[j] = (v, 1/rho) (the step's velocity array with 1/rho in w), and the next
+// group of four indices is fetched while the current group is processed.
 #pragma once
 #include "common.cuh"
 
@@ -37,33 +40,34 @@ __device__ __forceinline__ void force_pair(ForceAcc& A, const SimParams& P, floa
 // grid tables (the batched solver passes per-scene tables and P).
 template <int MODE>
 __device__ __forceinline__ void force_one(
-    uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel,
-    const float2* __restrict__ aux, const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
+    uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ xa,
+    const float4* __restrict__ va, const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     const SimParams& P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
     float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
-    const float4 xi = pos[i];
-    const float4 vi = vel[i];
-    const float2 ai = aux[i];
-    const float tcoef = P.tens_coef * ai.y;
+    const float4 xi = xa[i];  // (x, y, z, p/rho^2)
+    const float4 vi = va[i];  // (v, 1/rho)
+    const float tcoef = P.tens_coef * vi.w;
     ForceAcc A = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const uint32_t kc = nbr_count[i];
     if (kc <= (uint32_t)kMaxNbr) {
+        uint4 g = kc ? __ldg(&nbr4[i]) : make_uint4(0u, 0u, 0u, 0u);
         for (uint32_t t = 0; t < kc; t += 4) {
-            const uint4 g = __ldg(&nbr4[(size_t)(t >> 2) * n + i]);
+            const uint4 gn = (t + 4 < kc) ? __ldg(&nbr4[(size_t)((t >> 2) + 1) * n + i]) : g;
             const uint32_t js[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (t + u < kc) {
                     const uint32_t j = min(js[u], n - 1);
-                    const float4 xj = __ldg(&pos[j]);
+                    const float4 xj = __ldg(&xa[j]);
+                    const float4 vj = __ldg(&va[j]);
                     float dx, dy, dz;
                     float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
-                    force_pair(A, P, ai.x, tcoef, vi, dx, dy, dz, r2, __ldg(&aux[j]),
-                               __ldg(&vel[j]));
+                    force_pair(A, P, xi.w, tcoef, vi, dx, dy, dz, r2, make_float2(xj.w, vj.w), vj);
                 }
             }
+            g = gn;
         }
     } else {
         const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
@@ -74,12 +78,14 @@ __device__ __forceinline__ void force_one(
                     const uint2 r = __ldg(&cells[row + cx]);
                     const uint32_t e = min(r.y, n);
                     for (uint32_t j = r.x; j < e; ++j) {
-                        const float4 xj = __ldg(&pos[j]);
+                        const float4 xj = __ldg(&xa[j]);
                         float dx, dy, dz;
                         float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
-                        if (r2 < P.T && r2 != 0.0f)
-                            force_pair(A, P, ai.x, tcoef, vi, dx, dy, dz, r2, __ldg(&aux[j]),
-                                       __ldg(&vel[j]));
+                        if (r2 < P.T && r2 != 0.0f) {
+                            const float4 vj = __ldg(&va[j]);
+                            force_pair(A, P, xi.w, tcoef, vi, dx, dy, dz, r2,
+                                       make_float2(xj.w, vj.w), vj);
+                        }
                     }
                 }
             }
@@ -114,13 +120,14 @@ __device__ __forceinline__ void force_one(
                 }
             }
     }
-    const float vf = P.visc_coef * ai.y;
+    const float vf = P.visc_coef * vi.w;
     const float axx = fmaf(vf, A.wx, A.fx) + bx;
     const float ayy = fmaf(vf, A.wy, A.fy) + P.gravity + by;
     const float azz = fmaf(vf, A.wz, A.fz) + bz;
     if (MODE == 0) {
         float nvx = fmaf(dt, axx, vi.x), nvy = fmaf(dt, ayy, vi.y), nvz = fmaf(dt, azz, vi.z);
-        pos_out[i] = make_float4(fmaf(dt, nvx, xi.x), fmaf(dt, nvy, xi.y), fmaf(dt, nvz, xi.z), xi.w);
+        pos_out[i] = make_float4(fmaf(dt, nvx, xi.x), fmaf(dt, nvy, xi.y), fmaf(dt, nvz, xi.z),
+                                 pos[i].w);
         vel_out[i] = make_float4(nvx, nvy, nvz, 0.0f);
     } else {
         acc_out[3 * i + 0] = axx;
@@ -132,7 +139,7 @@ __device__ __forceinline__ void force_one(
 
 template <int MODE>
 __global__ void __launch_bounds__(256) force_kernel(
-    const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ aux,
+    const float4* __restrict__ pos, const float4* __restrict__ xa, const float4* __restrict__ va,
     const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
@@ -140,7 +147,7 @@ __global__ void __launch_bounds__(256) force_kernel(
     float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    force_one<MODE>(i, pos, vel, aux, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P, dt,
+    force_one<MODE>(i, pos, xa, va, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P, dt,
                     pos_out, vel_out, acc_out, nbr_b);
 }
 

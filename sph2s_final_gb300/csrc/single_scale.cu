@@ -27,7 +27,7 @@ int free_solver(sph_solver* s) {
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->err,     s->stage, s->nbr, s->nbr_count,
-                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb};
+                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
@@ -72,12 +72,13 @@ int enqueue_neighborhood(sph_solver* s) {
 
 void enqueue_density(sph_solver* s) {
     density_kernel<false><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
-        s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, nullptr);
+        s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, nullptr, s->xa,
+        s->svel);
 }
 
 void enqueue_force(sph_solver* s, float dt) {
     force_kernel<0><<<blocks_for(s->n), 256, 0, s->stream>>>(
-        s->spos, s->svel, s->aux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
+        s->spos, s->xa, s->svel, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
         s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr);
 }
 
@@ -89,9 +90,10 @@ void enqueue_step(sph_solver* s, float dt) {
     if (s->integrator == SPH_INTEGRATOR_XSPH) {
         // density (+ full neighbour counts), accelerations, XSPH integrate
         density_kernel<true><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
-            s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, s->xall);
+            s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, s->xall, s->xa,
+            s->svel);
         force_kernel<1><<<blocks_for(s->n), 256, 0, s->stream>>>(
-            s->spos, s->svel, s->aux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
+            s->spos, s->xa, s->svel, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
             s->n, s->nb, s->P, dt, nullptr, nullptr, s->xacc, s->xnb);
         xsph_integrate_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(
             s->spos, s->svel, s->xacc, s->aux, s->cells, s->nbr, s->nbr_count, s->xall, s->n, s->P,
@@ -167,6 +169,7 @@ int create_solver(const sph_config* config, const float4* hpos, const float4* hv
     TRY(dalloc(&s->svel, n_fluid));
     TRY(dalloc(&s->rho, n_fluid));
     TRY(dalloc(&s->aux, n_fluid));
+    TRY(dalloc(&s->xa, n_fluid));
     TRY(dalloc(&s->nbr, (size_t)n_fluid * (kMaxNbr / 4)));
     TRY(dalloc(&s->nbr_count, n_fluid));
     TRY(dalloc(&s->bnear, s->ncells));
@@ -442,9 +445,9 @@ int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t
     SPH_CUDA(cudaMalloc(&dnb, 4 * (size_t)n));
     enqueue_neighborhood(s);
     density_kernel<true><<<blocks_for(n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
-        s->spos, s->cells, n, s->P, drho, daux, s->nbr, s->nbr_count, dnf);
+        s->spos, s->cells, n, s->P, drho, daux, s->nbr, s->nbr_count, dnf, s->xa, s->svel);
     force_kernel<1><<<blocks_for(n), 256, 0, s->stream>>>(
-        s->spos, s->svel, daux, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear, n,
+        s->spos, s->xa, s->svel, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear, n,
         s->nb, s->P, 0.0f, nullptr, nullptr, dacc, dnb);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

@@ -22,6 +22,7 @@ struct sph_solver {
     float4* svel = nullptr;
     float* rho = nullptr;
     float2* aux = nullptr;
+    float4* xa = nullptr;           // force-pass records (x, p/rho^2), written by the density pass
     uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
     uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
     uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
