@@ -48,7 +48,7 @@ __device__ __forceinline__ void density_one(uint32_t i, const float4* __restrict
     const float4 xi = pos[i];
     // next list slot: element k & 3 of group k >> 2, i.e. u32 offset 4 (g n + i) + (k & 3)
     uint32_t* out = reinterpret_cast<uint32_t*>(nbr4) + 4 * (size_t)i;
-    const size_t next_group = 4 * (size_t)n - 3;
+    const uint32_t next_group = 4u * n - 3u;  // fits 32 bits: n <= 2^30
     const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
     for (int cz = s.z0; cz <= s.z1; ++cz)
         for (int cy = s.y0; cy <= s.y1; ++cy) {
@@ -65,7 +65,7 @@ __device__ __forceinline__ void density_one(uint32_t i, const float4* __restrict
                         sum = fmaf(a * a, a, sum);
                         if (r2 != 0.0f) {
                             if (k < (uint32_t)kMaxNbr) *out = j;
-                            out += (k & 3u) == 3u ? next_group : 1;
+                            out += (k & 3u) == 3u ? next_group : 1u;
                             ++k;
                         } else {
                             ++zero;
