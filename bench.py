@@ -335,6 +335,35 @@ def measure_batched_adjoint(num: int = 64, steps: int = 100, every: int = 20, re
                       "backward one scene after another"}
 
 
+def measure_two_scale(steps: int = 300, warmup: int = 20):
+    """Two-scale dam break (262,144 coarse particles at s = 1/128, refinement slab
+    0.35 < x < 0.65, blend increment 0.0125 per step, dt = 2.5e-5): wall time per
+    step of sph2_advance (synchronous: populations are read back every step) and
+    particle-steps/s over both populations, with the split / merge activity seen."""
+    from sph2s_final_gb300 import scenes
+    from sph2s_final_gb300.two_scale import Solver2
+
+    sc = scenes.two_scale_dam_break(1 / 128)
+    with Solver2(sc.low, None, sc.boundary, sc.config) as s:
+        s.advance(sc.dt, warmup)
+        part_steps, splits, merges = 0, 0, 0
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            c = s.counts()
+            part_steps += c["low"] + c["high"]
+            s.advance(sc.dt, 1)
+            st = s.last_stats()
+            splits += st["splits"]
+            merges += st["merges"]
+        el = time.perf_counter() - t0
+        c = s.counts()
+    return {"workload": "two-scale dam break, 262,144 coarse + fine children, slab 0.35<x<0.65, "
+                        "dt 2.5e-5", "steps": steps, "warmup": warmup,
+            "ms_per_step": 1e3 * el / steps, "particle_steps_per_s": part_steps / el,
+            "final_low": c["low"], "final_high": c["high"], "splits": splits, "merges": merges,
+            "timing": "host clock around synchronous sph2_advance calls"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -495,6 +524,7 @@ def run_ours(args):
         line["batched"] = measure_batched(args.batched_steps)
         line["adjoint"] = measure_adjoint()
         line["batched_adjoint"] = measure_batched_adjoint()
+        line["two_scale"] = measure_two_scale()
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -39,6 +39,8 @@ struct Pop {
     int32_t* istt = nullptr;
     uint32_t *igrp = nullptr, *keep = nullptr, *off = nullptr, *split = nullptr, *soff = nullptr;
     uint2* cells = nullptr;
+    uint4* list = nullptr;           // same-population force neighbours, kMaxNbr per particle
+    uint32_t* list_count = nullptr;
 };
 
 template <class T>
@@ -158,7 +160,9 @@ int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, std::vector<void*>& o) {
         (rc = dalloc(&p.istt, cap, o)) || (rc = dalloc(&p.igrp, cap, o)) ||
         (rc = dalloc(&p.keep, cap, o)) || (rc = dalloc(&p.off, cap, o)) ||
         (rc = dalloc(&p.split, cap, o)) || (rc = dalloc(&p.soff, cap, o)) ||
-        (rc = dalloc(&p.cells, p.ncells, o)))
+        (rc = dalloc(&p.cells, p.ncells, o)) ||
+        (rc = dalloc(&p.list, (size_t)cap * (kMaxNbr / 4), o)) ||
+        (rc = dalloc(&p.list_count, cap, o)))
         return rc;
     return SPH_OK;
 }
@@ -220,21 +224,21 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         if (debug && dbg_pop == 1)
             ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, dnb_same, dnb_compl,
-                H.sgrp, gb, s->gsum);
+                H.sgrp, gb, s->gsum, H.list, H.list_count);
         else
             ts_density_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, nullptr, nullptr,
-                H.sgrp, gb, s->gsum);
+                H.sgrp, gb, s->gsum, H.list, H.list_count);
     }
     if (L.n) {
         if (debug && dbg_pop == 0)
             ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl,
-                L.sgrp, gb, s->gsum);
+                L.sgrp, gb, s->gsum, L.list, L.list_count);
         else
             ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr,
-                L.sgrp, gb, s->gsum);
+                L.sgrp, gb, s->gsum, L.list, L.list_count);
     }
     // merge decisions (slab: start-of-step centroids; surface: this step's densities)
     if (gb && (s->P.axis >= 0 || s->P.surface))
@@ -248,22 +252,22 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         if (debug && dbg_pop == 1)
             ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, o);
         else
             ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, o);
     }
     if (L.n) {
         TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
             ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, o);
         else
             ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, o);
     }
 }
 

@@ -132,13 +132,19 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
     const float4* __restrict__ spos_c, const uint2* __restrict__ cells_c, uint32_t n_c,
     TSParams P, float* __restrict__ rho, float2* __restrict__ aux, uint32_t* __restrict__ nbr_same,
     uint32_t* __restrict__ nbr_compl, const uint32_t* __restrict__ sgrp_r, uint32_t group_base,
-    unsigned long long* __restrict__ gsurf) {
+    unsigned long long* __restrict__ gsurf, uint4* __restrict__ list4,
+    uint32_t* __restrict__ list_count) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
     const float4 xi = spos_r[i];
     float s = 0.0f, sc = 0.0f;
     uint32_t ns = 0, nc = 0;
+    // same-population force neighbours (0 < r2 < T_r) in stencil order, grouped
+    // layout: element k & 3 of group k >> 2 at u32 offset 4 (g n + i) + (k & 3)
+    uint32_t k = 0;
+    uint32_t* out = reinterpret_cast<uint32_t*>(list4) + 4 * (size_t)i;
+    const uint32_t next_group = 4u * n_r - 3u;
     {
         const Stencil st = stencil(P.g[R], xi.x, xi.y, xi.z, P.h[R]);
         for (int cz = st.z0; cz <= st.z1; ++cz)
@@ -155,6 +161,11 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                             const float a = P.h2[R] - r2;
                             s = fmaf(P.coupled ? 1.0f : xj.w, a * a * a, s);
                             if (DEBUG) ++ns;
+                            if (r2 != 0.0f) {
+                                if (k < (uint32_t)kMaxNbr) *out = j;
+                                out += (k & 3u) == 3u ? next_group : 1u;
+                                ++k;
+                            }
                         }
                     }
                 }
@@ -188,6 +199,7 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
     const float inv = 1.0f / rh;
     rho[i] = rh;
     aux[i] = make_float2(p * inv * inv, inv);
+    list_count[i] = k;
     if (DEBUG) {
         nbr_same[i] = ns;
         nbr_compl[i] = nc;
@@ -222,7 +234,8 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells, uint32_t nb, TSParams P,
     float dt, const uint32_t* __restrict__ gmerge, uint32_t n_groups,
     unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl,
-    const float* __restrict__ rho_r, TSOut out) {
+    const float* __restrict__ rho_r, const uint4* __restrict__ list4,
+    const uint32_t* __restrict__ list_count, TSOut out) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -240,48 +253,70 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     {
         const float tco = P.sigma * P.mass[R] * P.poly6[R] * ai.y;
         const float pco = P.mass[R] * P.spiky[R];
-        const Stencil st = stencil(P.g[R], xi.x, xi.y, xi.z, P.h[R]);
-        for (int cz = st.z0; cz <= st.z1; ++cz)
-            for (int cy = st.y0; cy <= st.y1; ++cy) {
-                const uint32_t row = linear_cell(P.g[R], 0, cy, cz);
-                for (int cx = st.x0; cx <= st.x1; ++cx) {
-                    const uint2 r = __ldg(&cells_r[row + cx]);
-                    const uint32_t e = min(r.y, n_r);
-                    for (uint32_t j = r.x; j < e; ++j) {
+        // one same-population neighbour j (0 < r2 < T_r)
+        auto pair = [&](uint32_t j, const float4& xj, float dx, float dy, float dz, float r2) {
+            const float2 aj = __ldg(&aux_r[j]);
+            const float4 vj = __ldg(&svel_r[j]);
+            const float rs = rsqrtf(r2);
+            const float hr = P.h[R] - r2 * rs;
+            const float a = P.h2[R] - r2;
+            const float lj = P.coupled ? 1.0f : xj.w;
+            const float sc = lj * (pco * (ai.x + aj.x) * hr * hr * rs - tco * a * a * a);
+            fx = fmaf(sc, dx, fx);
+            fy = fmaf(sc, dy, fy);
+            fz = fmaf(sc, dz, fz);
+            const float vc = lj * aj.y * hr * P.spiky[R] * P.mass[R];
+            wx = fmaf(vc, vj.x - vi.x, wx);
+            wy = fmaf(vc, vj.y - vi.y, wy);
+            wz = fmaf(vc, vj.z - vi.z, wz);
+            if (colour) {
+                const float q2 = r2 * inv_h2;
+                const float psi = kMexicanHatC * (q2 - 3.0f) * expf(-0.5f * q2);
+                psum += psi;
+                cwx = fmaf(vj.x, psi, cwx);
+                cwy = fmaf(vj.y, psi, cwy);
+                cwz = fmaf(vj.z, psi, cwz);
+                csx += xj.x;
+                csy += xj.y;
+                csz += xj.z;
+                ccnt += 1.0f;
+            }
+        };
+        const uint32_t kc = list_count[i];
+        if (kc <= (uint32_t)kMaxNbr) {  // the density pass's list, in stencil order
+            uint4 g = kc ? __ldg(&list4[i]) : make_uint4(0u, 0u, 0u, 0u);
+            for (uint32_t t = 0; t < kc; t += 4) {
+                const uint4 gn = (t + 4 < kc) ? __ldg(&list4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
+                const uint32_t js[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (t + u < kc) {
+                        const uint32_t j = min(js[u], n_r - 1);
                         const float4 xj = __ldg(&spos_r[j]);
                         float dx, dy, dz;
                         const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
-                        if (r2 < P.T[R] && r2 != 0.0f) {
-                            const float2 aj = __ldg(&aux_r[j]);
-                            const float4 vj = __ldg(&svel_r[j]);
-                            const float rs = rsqrtf(r2);
-                            const float hr = P.h[R] - r2 * rs;
-                            const float a = P.h2[R] - r2;
-                            const float lj = P.coupled ? 1.0f : xj.w;
-                            const float sc = lj * (pco * (ai.x + aj.x) * hr * hr * rs - tco * a * a * a);
-                            fx = fmaf(sc, dx, fx);
-                            fy = fmaf(sc, dy, fy);
-                            fz = fmaf(sc, dz, fz);
-                            const float vc = lj * aj.y * hr * P.spiky[R] * P.mass[R];
-                            wx = fmaf(vc, vj.x - vi.x, wx);
-                            wy = fmaf(vc, vj.y - vi.y, wy);
-                            wz = fmaf(vc, vj.z - vi.z, wz);
-                            if (colour) {
-                                const float q2 = r2 * inv_h2;
-                                const float psi = kMexicanHatC * (q2 - 3.0f) * expf(-0.5f * q2);
-                                psum += psi;
-                                cwx = fmaf(vj.x, psi, cwx);
-                                cwy = fmaf(vj.y, psi, cwy);
-                                cwz = fmaf(vj.z, psi, cwz);
-                                csx += xj.x;
-                                csy += xj.y;
-                                csz += xj.z;
-                                ccnt += 1.0f;
-                            }
+                        pair(j, xj, dx, dy, dz, r2);
+                    }
+                }
+                g = gn;
+            }
+        } else {
+            const Stencil st = stencil(P.g[R], xi.x, xi.y, xi.z, P.h[R]);
+            for (int cz = st.z0; cz <= st.z1; ++cz)
+                for (int cy = st.y0; cy <= st.y1; ++cy) {
+                    const uint32_t row = linear_cell(P.g[R], 0, cy, cz);
+                    for (int cx = st.x0; cx <= st.x1; ++cx) {
+                        const uint2 r = __ldg(&cells_r[row + cx]);
+                        const uint32_t e = min(r.y, n_r);
+                        for (uint32_t j = r.x; j < e; ++j) {
+                            const float4 xj = __ldg(&spos_r[j]);
+                            float dx, dy, dz;
+                            const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+                            if (r2 < P.T[R] && r2 != 0.0f) pair(j, xj, dx, dy, dz, r2);
                         }
                     }
                 }
-            }
+        }
     }
     if (n_c > 0) {
         const Stencil st = stencil(P.g[C], xi.x, xi.y, xi.z, P.h[0]);
