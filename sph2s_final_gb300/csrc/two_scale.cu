@@ -41,6 +41,8 @@ struct Pop {
     uint2* cells = nullptr;
     uint4* list = nullptr;           // same-population force neighbours, kMaxNbr per particle
     uint32_t* list_count = nullptr;
+    uint4* clist = nullptr;          // complementary force neighbours, ComplCap per particle
+    uint32_t* clist_count = nullptr;
 };
 
 template <class T>
@@ -146,7 +148,7 @@ int make_ts_params(const sph_config2& c, TSParams* out) {
     return SPH_OK;
 }
 
-int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, std::vector<void*>& o) {
+int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, uint32_t compl_cap, std::vector<void*>& o) {
     p.cap = cap;
     p.ncells = sph_grid_num_cells(&g);
     p.key_bits = 3 * morton_bits_for(g);
@@ -162,7 +164,9 @@ int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, std::vector<void*>& o) {
         (rc = dalloc(&p.split, cap, o)) || (rc = dalloc(&p.soff, cap, o)) ||
         (rc = dalloc(&p.cells, p.ncells, o)) ||
         (rc = dalloc(&p.list, (size_t)cap * (kMaxNbr / 4), o)) ||
-        (rc = dalloc(&p.list_count, cap, o)))
+        (rc = dalloc(&p.list_count, cap, o)) ||
+        (rc = dalloc(&p.clist, (size_t)cap * (compl_cap / 4), o)) ||
+        (rc = dalloc(&p.clist_count, cap, o)))
         return rc;
     return SPH_OK;
 }
@@ -224,21 +228,21 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         if (debug && dbg_pop == 1)
             ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, dnb_same, dnb_compl,
-                H.sgrp, gb, s->gsum, H.list, H.list_count);
+                H.sgrp, gb, s->gsum, H.list, H.list_count, H.clist, H.clist_count);
         else
             ts_density_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.cells, H.n, L.spos, L.cells, L.n, s->P, H.rho, H.aux, nullptr, nullptr,
-                H.sgrp, gb, s->gsum, H.list, H.list_count);
+                H.sgrp, gb, s->gsum, H.list, H.list_count, H.clist, H.clist_count);
     }
     if (L.n) {
         if (debug && dbg_pop == 0)
             ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl,
-                L.sgrp, gb, s->gsum, L.list, L.list_count);
+                L.sgrp, gb, s->gsum, L.list, L.list_count, L.clist, L.clist_count);
         else
             ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr,
-                L.sgrp, gb, s->gsum, L.list, L.list_count);
+                L.sgrp, gb, s->gsum, L.list, L.list_count, L.clist, L.clist_count);
     }
     // merge decisions (slab: start-of-step centroids; surface: this step's densities)
     if (gb && (s->P.axis >= 0 || s->P.surface))
@@ -252,22 +256,22 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         if (debug && dbg_pop == 1)
             ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
         else
             ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, o);
+                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
     }
     if (L.n) {
         TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
             ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
         else
             ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, o);
+                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
     }
 }
 
@@ -401,8 +405,8 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
         return fail(SPH_E_INVALID, "two-scale state: group counter beyond the group capacity");
     }
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
-    TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], s->owned));
-    TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], s->owned));
+    TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], ComplCap<0>::value, s->owned));
+    TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], ComplCap<1>::value, s->owned));
     const uint32_t nmax = (uint32_t)std::max<uint64_t>(std::max(capL, capH), n_boundary);
     for (int b = 0; b < 2; ++b) {
         TRY(dalloc(&s->keys[b], nmax, s->owned));

@@ -16,6 +16,13 @@
 namespace sph {
 
 constexpr uint32_t kNoGroup = 0xFFFFFFFFu;
+// Complementary-neighbour list capacity per particle: a LOW particle inside a
+// refined region has ~8x34 fine neighbours within its support, a HIGH
+// particle at most ~40 coarse ones.  Particles beyond it rescan the stencil.
+template <int R>
+struct ComplCap {
+    static constexpr uint32_t value = R == 0 ? 320u : 64u;
+};
 
 struct TSParams {
     GridParams g[2];
@@ -133,7 +140,8 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
     TSParams P, float* __restrict__ rho, float2* __restrict__ aux, uint32_t* __restrict__ nbr_same,
     uint32_t* __restrict__ nbr_compl, const uint32_t* __restrict__ sgrp_r, uint32_t group_base,
     unsigned long long* __restrict__ gsurf, uint4* __restrict__ list4,
-    uint32_t* __restrict__ list_count) {
+    uint32_t* __restrict__ list_count, uint4* __restrict__ clist4,
+    uint32_t* __restrict__ clist_count) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -171,6 +179,9 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                 }
             }
     }
+    // complementary force neighbours (0 < r2 < T_0) in stencil order, same layout
+    uint32_t kcl = 0;
+    uint32_t* cout = reinterpret_cast<uint32_t*>(clist4) + 4 * (size_t)i;
     if (n_c > 0) {
         const Stencil st = stencil(P.g[C], xi.x, xi.y, xi.z, P.h[0]);
         for (int cz = st.z0; cz <= st.z1; ++cz)
@@ -189,11 +200,17 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                             if (r2 < P.T[1]) w += P.poly6[1] * a1 * a1 * a1;
                             sc = fmaf(P.coupled ? 1.0f : xj.w, 0.5f * w, sc);
                             if (DEBUG) ++nc;
+                            if (r2 != 0.0f) {
+                                if (kcl < ComplCap<R>::value) *cout = j;
+                                cout += (kcl & 3u) == 3u ? next_group : 1u;
+                                ++kcl;
+                            }
                         }
                     }
                 }
             }
     }
+    clist_count[i] = kcl;
     const float rh = P.mass[R] * P.poly6[R] * s + P.mass[C] * sc;
     const float p = P.bulk * (rh - P.rho0);
     const float inv = 1.0f / rh;
@@ -235,7 +252,8 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     float dt, const uint32_t* __restrict__ gmerge, uint32_t n_groups,
     unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl,
     const float* __restrict__ rho_r, const uint4* __restrict__ list4,
-    const uint32_t* __restrict__ list_count, TSOut out) {
+    const uint32_t* __restrict__ list_count, const uint4* __restrict__ clist4,
+    const uint32_t* __restrict__ clist_count, TSOut out) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -319,52 +337,72 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         }
     }
     if (n_c > 0) {
-        const Stencil st = stencil(P.g[C], xi.x, xi.y, xi.z, P.h[0]);
-        for (int cz = st.z0; cz <= st.z1; ++cz)
-            for (int cy = st.y0; cy <= st.y1; ++cy) {
-                const uint32_t row = linear_cell(P.g[C], 0, cy, cz);
-                for (int cx = st.x0; cx <= st.x1; ++cx) {
-                    const uint2 r = __ldg(&cells_c[row + cx]);
-                    const uint32_t e = min(r.y, n_c);
-                    for (uint32_t j = r.x; j < e; ++j) {
+        // one complementary neighbour j (0 < r2 < T_0)
+        auto cpair = [&](uint32_t j, const float4& xj, float dx, float dy, float dz, float r2) {
+            const float2 aj = __ldg(&aux_c[j]);
+            const float4 vj = __ldg(&svel_c[j]);
+            const float rs = rsqrtf(r2);
+            const float rr = r2 * rs;
+            const bool in1 = r2 < P.T[1];
+            const float h0r = P.h[0] - rr, h1r = P.h[1] - rr;
+            const float a0 = P.h2[0] - r2, a1 = P.h2[1] - r2;
+            float g = P.spiky[0] * h0r * h0r;
+            float l = P.spiky[0] * h0r;
+            float w = P.poly6[0] * a0 * a0 * a0;
+            if (in1) {
+                g += P.spiky[1] * h1r * h1r;
+                l += P.spiky[1] * h1r;
+                w += P.poly6[1] * a1 * a1 * a1;
+            }
+            // coupled: the neighbour support's Poly6 for tension
+            // (SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu:448-460)
+            const float wt = !P.coupled ? 0.5f * w
+                                        : (C == 0 ? P.poly6[0] * a0 * a0 * a0
+                                                  : (in1 ? P.poly6[1] * a1 * a1 * a1 : 0.0f));
+            const float lj = P.coupled ? 1.0f : xj.w;
+            const float sc = lj * (P.mass[C] * (ai.x + aj.x) * 0.5f * g * rs -
+                                   P.sigma * P.mass[C] * wt * ai.y);
+            fx = fmaf(sc, dx, fx);
+            fy = fmaf(sc, dy, fy);
+            fz = fmaf(sc, dz, fz);
+            const float vc = lj * P.mass[C] * aj.y * 0.5f * l;
+            wx = fmaf(vc, vj.x - vi.x, wx);
+            wy = fmaf(vc, vj.y - vi.y, wy);
+            wz = fmaf(vc, vj.z - vi.z, wz);
+        };
+        const uint32_t kc = clist_count[i];
+        if (kc <= ComplCap<R>::value) {  // the density pass's list, in stencil order
+            for (uint32_t t = 0; t < kc; t += 4) {
+                const uint4 g = __ldg(&clist4[(size_t)(t >> 2) * n_r + i]);
+                const uint32_t js[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (t + u < kc) {
+                        const uint32_t j = min(js[u], n_c - 1);
                         const float4 xj = __ldg(&spos_c[j]);
                         float dx, dy, dz;
                         const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
-                        if (r2 < P.T[0] && r2 != 0.0f) {
-                            const float2 aj = __ldg(&aux_c[j]);
-                            const float4 vj = __ldg(&svel_c[j]);
-                            const float rs = rsqrtf(r2);
-                            const float rr = r2 * rs;
-                            const bool in1 = r2 < P.T[1];
-                            const float h0r = P.h[0] - rr, h1r = P.h[1] - rr;
-                            const float a0 = P.h2[0] - r2, a1 = P.h2[1] - r2;
-                            float g = P.spiky[0] * h0r * h0r;
-                            float l = P.spiky[0] * h0r;
-                            float w = P.poly6[0] * a0 * a0 * a0;
-                            if (in1) {
-                                g += P.spiky[1] * h1r * h1r;
-                                l += P.spiky[1] * h1r;
-                                w += P.poly6[1] * a1 * a1 * a1;
-                            }
-                            // coupled: the neighbour support's Poly6 for tension
-                            // (SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu:448-460)
-                            const float wt = !P.coupled ? 0.5f * w
-                                                        : (C == 0 ? P.poly6[0] * a0 * a0 * a0
-                                                                  : (in1 ? P.poly6[1] * a1 * a1 * a1 : 0.0f));
-                            const float lj = P.coupled ? 1.0f : xj.w;
-                            const float sc = lj * (P.mass[C] * (ai.x + aj.x) * 0.5f * g * rs -
-                                                   P.sigma * P.mass[C] * wt * ai.y);
-                            fx = fmaf(sc, dx, fx);
-                            fy = fmaf(sc, dy, fy);
-                            fz = fmaf(sc, dz, fz);
-                            const float vc = lj * P.mass[C] * aj.y * 0.5f * l;
-                            wx = fmaf(vc, vj.x - vi.x, wx);
-                            wy = fmaf(vc, vj.y - vi.y, wy);
-                            wz = fmaf(vc, vj.z - vi.z, wz);
-                        }
+                        cpair(j, xj, dx, dy, dz, r2);
                     }
                 }
             }
+        } else {
+            const Stencil st = stencil(P.g[C], xi.x, xi.y, xi.z, P.h[0]);
+            for (int cz = st.z0; cz <= st.z1; ++cz)
+                for (int cy = st.y0; cy <= st.y1; ++cy) {
+                    const uint32_t row = linear_cell(P.g[C], 0, cy, cz);
+                    for (int cx = st.x0; cx <= st.x1; ++cx) {
+                        const uint2 r = __ldg(&cells_c[row + cx]);
+                        const uint32_t e = min(r.y, n_c);
+                        for (uint32_t j = r.x; j < e; ++j) {
+                            const float4 xj = __ldg(&spos_c[j]);
+                            float dx, dy, dz;
+                            const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+                            if (r2 < P.T[0] && r2 != 0.0f) cpair(j, xj, dx, dy, dz, r2);
+                        }
+                    }
+                }
+        }
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
     uint32_t bcnt = 0;
