@@ -102,6 +102,47 @@ def test_merge_path_matches():
         assert merges > 0
 
 
+SLAB_RUNS = {
+    # a narrow slab that fine particles cross both ways: every event occurs
+    "crossing": (dict(spacing=1 / 32, dt=2e-4, slab=(0.40, 0.485), blend_increment=0.25),
+                 ("splits", "merges", "removed_low", "removed_high", "faded_in_low",
+                  "faded_in_high")),
+    # the 262,144-particle two-scale configuration's slab 0.35 < x < 0.65 and
+    # blend increment 0.0125 at 32,768 coarse particles (dt scaled with h)
+    "c2_slab": (dict(spacing=1 / 64, dt=5e-5), ("splits", "removed_low", "faded_in_high")),
+}
+
+
+@pytest.mark.parametrize("run", sorted(SLAB_RUNS))
+def test_split_merge_counts_every_step_for_1000_steps(run):
+    """1,000 consecutive steps: before every step the oracle takes the GPU's
+    state; after it the split, merge, removal and fade-in counts, population
+    sizes, persistent ids, states, blend coefficients and group ids match bit
+    for bit."""
+    kw, seen = SLAB_RUNS[run]
+    kw = dict(kw)
+    sc = scenes.two_scale_dam_break(kw.pop("spacing"), **kw)
+    totals = dict.fromkeys(("splits", "merges", "removed_low", "removed_high", "faded_in_low",
+                            "faded_in_high"), 0)
+    with Solver2(sc.low, None, sc.boundary, sc.config) as s:
+        for k in range(1000):
+            ro, _ = oracle_from_gpu(s, sc)
+            ro.advance(sc.dt, 1)
+            s.advance(sc.dt, 1)
+            st = s.last_stats()
+            assert st == ro.last_stats(), k
+            c, oc = s.counts(), ro.counts()
+            assert (c["low"], c["high"], c["groups"]) == (oc["low"], oc["high"], oc["groups"]), k
+            for r in (LOW, HIGH):
+                g, o = s.state(r), ro.state(r)
+                for key in ("ids", "state", "group", "lam"):
+                    np.testing.assert_array_equal(g[key], o[key], err_msg=f"step {k} {key}")
+            ro.close()
+            for key, v in st.items():
+                totals[key] += v
+    assert all(totals[key] > 0 for key in seen), totals
+
+
 def test_without_refinement_is_two_independent_populations(small):
     cfg = small.config
     cfg.refine_axis = -1
