@@ -64,6 +64,7 @@ struct sph_solver2 {
     uint32_t nb = 0;
     float4* bpos = nullptr;
     uint2* bcells = nullptr;
+    uint8_t* bnear = nullptr;  // per LOW cell: a boundary particle within stencil reach
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
     void* sort_mem = nullptr;
@@ -256,22 +257,22 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         if (debug && dbg_pop == 1)
             ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
+                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
         else
             ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
+                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
     }
     if (L.n) {
         TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
             ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
+                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
         else
             ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
+                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
     }
 }
 
@@ -426,6 +427,7 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
     TRY(dalloc(&s->err, 1, s->owned));
     TRY(dalloc(&s->bpos, n_boundary, s->owned));
     TRY(dalloc(&s->bcells, s->pop[0].ncells, s->owned));
+    TRY(dalloc(&s->bnear, s->pop[0].ncells, s->owned));
     TRY(check_cuda(cudaMallocHost((void**)&s->ctl_host, 4 * kCtlWords), "pinned", __FILE__, __LINE__));
     TRY(check_cuda(cudaMemset(s->err, 0, 4), "memset", __FILE__, __LINE__));
     {
@@ -465,6 +467,13 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
         }
         if (braw) cudaFree(braw);
         TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
+    }
+    {
+        const int reach = (int)std::ceil(s->cfg.effective_radius[0] / s->cfg.grid[0].spacing) + 1;
+        boundary_near_kernel<<<blocks_for(s->pop[0].ncells), 256, 0, s->stream>>>(
+            s->bcells, s->P.g[0], reach, s->bnear);
+        TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
+        TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
     }
     TRY(check_err2(s));
 #undef TRY

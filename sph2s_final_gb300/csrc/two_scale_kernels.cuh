@@ -248,7 +248,8 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     const float2* __restrict__ aux_r, const uint2* __restrict__ cells_r, uint32_t n_r,
     const float4* __restrict__ spos_c, const float4* __restrict__ svel_c,
     const float2* __restrict__ aux_c, const uint2* __restrict__ cells_c, uint32_t n_c,
-    const float4* __restrict__ bpos, const uint2* __restrict__ bcells, uint32_t nb, TSParams P,
+    const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
+    const uint8_t* __restrict__ bnear, uint32_t nb, TSParams P,
     float dt, const uint32_t* __restrict__ gmerge, uint32_t n_groups,
     unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl,
     const float* __restrict__ rho_r, const uint4* __restrict__ list4,
@@ -372,8 +373,10 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         };
         const uint32_t kc = clist_count[i];
         if (kc <= ComplCap<R>::value) {  // the density pass's list, in stencil order
+            uint4 gc = kc ? __ldg(&clist4[i]) : make_uint4(0u, 0u, 0u, 0u);
             for (uint32_t t = 0; t < kc; t += 4) {
-                const uint4 g = __ldg(&clist4[(size_t)(t >> 2) * n_r + i]);
+                const uint4 g = gc;  // this group; the next one is fetched meanwhile
+                gc = (t + 4 < kc) ? __ldg(&clist4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
                 const uint32_t js[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
@@ -406,7 +409,12 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
     uint32_t bcnt = 0;
-    {
+    // the boundary stencil lives on the LOW grid; particles of LOW cells with no
+    // boundary particle within stencil reach skip it (bnear, set once at creation)
+    const uint32_t bhome = linear_cell(P.g[0], cell_coord(xi.x, P.g[0].ox, P.g[0].spacing, P.g[0].dx),
+                                       cell_coord(xi.y, P.g[0].oy, P.g[0].spacing, P.g[0].dy),
+                                       cell_coord(xi.z, P.g[0].oz, P.g[0].spacing, P.g[0].dz));
+    if (__ldg(&bnear[bhome])) {
         const Stencil st = stencil(P.g[0], xi.x, xi.y, xi.z, P.h[0]);
         for (int cz = st.z0; cz <= st.z1; ++cz)
             for (int cy = st.y0; cy <= st.y1; ++cy) {
