@@ -186,28 +186,35 @@ TSOut outputs(Pop& p, float* acc, uint32_t* nbr_bnd, float* colour = nullptr) {
     return o;
 }
 
-// hash -> sort -> reorder + cell ranges of population r (Solver.cu:1616-1680).
-void ts_neighborhood(sph_solver2* s, int r) {
-    Pop& p = s->pop[r];
+// hash -> sort -> reorder + cell ranges of both populations (Solver.cu:1616-1680):
+// one stable sort of (population bit, cell key) pairs gives each population the
+// order of its own sort with half the sort launches.
+void ts_neighborhoods(sph_solver2* s) {
+    Pop &L = s->pop[0], &H = s->pop[1];
     cudaStream_t st = s->stream;
-    cudaMemsetAsync(p.cells, 0xFF, sizeof(uint2) * p.ncells, st);
-    if (p.n == 0) return;
-    const int passes = sort_passes(p.key_bits);
+    cudaMemsetAsync(H.cells, 0xFF, sizeof(uint2) * H.ncells, st);
+    cudaMemsetAsync(L.cells, 0xFF, sizeof(uint2) * L.ncells, st);
+    const uint32_t n = L.n + H.n;
+    if (n == 0) return;
+    const int pop_bit = std::max(L.key_bits, H.key_bits);
+    const int passes = sort_passes(pop_bit + 1);
     sort_reset(s->sort, st);
-    uint32_t hb = blocks_for(p.n);
+    uint32_t hb = blocks_for(n);
     if (hb > 1216) hb = 1216;
-    hash_hist_kernel<<<hb, 256, 0, st>>>(p.pos, p.n, s->P.g[r], passes, s->keys[0], s->sort.hist);
+    ts_hash_hist_kernel<<<hb, 256, 0, st>>>(L.pos, L.n, s->P.g[0], H.pos, H.n, s->P.g[1], pop_bit,
+                                            passes, s->keys[0], s->sort.hist);
     sort_scan(passes, s->sort, st);
-    const int o = sort_passes_run(s->keys, s->vals, nullptr, p.n, passes, s->sort, s->err, 0, st);
-    if (r == 1)
-        ts_gather_kernel<true><<<blocks_for(p.n), 256, 0, st>>>(
-            s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
-            p.sstt, p.sgrp, p.cells, s->err, s->P.axis, s->P.surface, s->group_base, s->gsum,
-            s->gready);
-    else
-        ts_gather_kernel<false><<<blocks_for(p.n), 256, 0, st>>>(
-            s->keys[o], s->vals[o], p.n, s->P.g[r], p.pos, p.vel, p.stt, p.grp, p.spos, p.svel,
-            p.sstt, p.sgrp, p.cells, s->err, -1, 0, 0, nullptr, nullptr);
+    const int o = sort_passes_run(s->keys, s->vals, nullptr, n, passes, s->sort, s->err, 0, st);
+    const uint32_t mask = (1u << pop_bit) - 1u;
+    if (H.n)
+        ts_gather_kernel<true><<<blocks_for(H.n), 256, 0, st>>>(
+            s->keys[o] + L.n, s->vals[o] + L.n, H.n, mask, L.n, s->P.g[1], H.pos, H.vel, H.stt,
+            H.grp, H.spos, H.svel, H.sstt, H.sgrp, H.cells, s->err, s->P.axis, s->P.surface,
+            s->group_base, s->gsum, s->gready);
+    if (L.n)
+        ts_gather_kernel<false><<<blocks_for(L.n), 256, 0, st>>>(
+            s->keys[o], s->vals[o], L.n, mask, 0u, s->P.g[0], L.pos, L.vel, L.stt, L.grp, L.spos,
+            L.svel, L.sstt, L.sgrp, L.cells, s->err, -1, 0, 0, nullptr, nullptr);
 }
 
 // Everything up to and including the force/integrate pass; DEBUG variants
@@ -222,8 +229,7 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         cudaMemsetAsync(s->gacc, 0, 48 * (size_t)gb, st);
     }
     cudaMemsetAsync(s->ctl + kCtlFadedL, 0, 8, st);
-    ts_neighborhood(s, 1);
-    ts_neighborhood(s, 0);
+    ts_neighborhoods(s);
     Pop &L = s->pop[0], &H = s->pop[1];
     if (H.n) {
         if (debug && dbg_pop == 1)
@@ -383,6 +389,9 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
                    const HostPop* pops, const float4* hb, uint32_t n_boundary,
                    uint32_t group_base, const uint32_t next_id[2], uint64_t step,
                    sph_solver2** out) {
+    // both populations share one sort, whose look-back counts hold 30 bits
+    if (capL + capH > kMaxParticles || n_boundary > kMaxParticles)
+        return fail(SPH_E_CAPACITY, "two-scale: more than 2^30 particles");
     sph_solver2* s = new sph_solver2();
     s->cfg = *config;
     s->P = P;
@@ -408,7 +417,8 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
     TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], ComplCap<0>::value, s->owned));
     TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], ComplCap<1>::value, s->owned));
-    const uint32_t nmax = (uint32_t)std::max<uint64_t>(std::max(capL, capH), n_boundary);
+    // one sort holds both populations (ts_neighborhoods), or the boundary at creation
+    const uint32_t nmax = (uint32_t)std::max<uint64_t>(capL + capH, n_boundary);
     for (int b = 0; b < 2; ++b) {
         TRY(dalloc(&s->keys[b], nmax, s->owned));
         TRY(dalloc(&s->vals[b], nmax, s->owned));
@@ -538,7 +548,7 @@ int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
     uint64_t capL = capacity_low ? capacity_low : 2ull * n_low + 1024;
     uint64_t capH = capacity_high ? capacity_high : 8ull * (n_low + n_high) + 1024;
     if (capL < n_low || capH < n_high) return fail(SPH_E_CAPACITY, "sph2_create: capacity below the initial count");
-    if (capL > kMaxParticles || capH > kMaxParticles || n_boundary > kMaxParticles)
+    if (capL + capH > kMaxParticles || n_boundary > kMaxParticles)
         return fail(SPH_E_CAPACITY, "sph2_create: more than 2^30 particles");
     HostPop pops[2] = {initial_pop(0, low_xyz, n_low), initial_pop(1, high_xyz, n_high)};
     std::vector<float4> hb(n_boundary);

@@ -68,11 +68,46 @@ __device__ __forceinline__ long long fixed40(float x) {
     return __double2ll_rn((double)x * 1099511627776.0);
 }
 
-// Reorder + cell ranges for one population; for HIGH also accumulates the
-// group centroid (slab axis, fixed point) and the number of members in state 4.
+// Cell keys of both populations for one stable sort: LOW keys on the LOW
+// grid, HIGH keys on the HIGH grid with bit `pop_bit` set, so the sorted
+// array is [LOW, HIGH], each part in the order a sort of its own would give
+// (SPH2S_FINAL_TWO_SCALE/Solver.cu:594-617, 1616-1661 sorts them one by one).
+// Input index i < n_l is LOW particle i, otherwise HIGH particle i - n_l.
+static __global__ void __launch_bounds__(256) ts_hash_hist_kernel(
+    const float4* __restrict__ pos_l, uint32_t n_l, GridParams g_l,
+    const float4* __restrict__ pos_h, uint32_t n_h, GridParams g_h, int pop_bit, int passes,
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kSortMaxPasses][256];
+    for (int i = threadIdx.x; i < kSortMaxPasses * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t n = n_l + n_h;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k;
+        if (i < n_l) {
+            const float4 p = pos_l[i];
+            k = cell_key(g_l, p.x, p.y, p.z);
+        } else {
+            const float4 p = pos_h[i - n_l];
+            k = cell_key(g_h, p.x, p.y, p.z) | (1u << pop_bit);
+        }
+        keys[i] = k;
+        sort_hist_add(sh, k, passes);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// Reorder + cell ranges for one population's part of the sorted array (keys
+// masked by key_mask, sorted values minus val_base are its indices); for HIGH
+// also accumulates the group centroid (slab axis, fixed point) and the number
+// of members in state 4.
 template <bool HIGH_POP>
 __global__ void __launch_bounds__(256) ts_gather_kernel(
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
+    uint32_t key_mask, uint32_t val_base,
     GridParams g, const float4* __restrict__ pos, const float4* __restrict__ vel,
     const int32_t* __restrict__ stt, const uint32_t* __restrict__ grp, float4* __restrict__ spos,
     float4* __restrict__ svel, int32_t* __restrict__ sstt, uint32_t* __restrict__ sgrp,
@@ -80,7 +115,7 @@ __global__ void __launch_bounds__(256) ts_gather_kernel(
     uint32_t group_base, unsigned long long* __restrict__ gsum, uint32_t* __restrict__ gready) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t q = perm[i];
+    uint32_t q = perm[i] - val_base;
     if (q >= n) {
         atomicOr(err, 2u);
         q = i;
@@ -99,17 +134,18 @@ __global__ void __launch_bounds__(256) ts_gather_kernel(
         }
         if (s == 4) atomicAdd(&gready[gid], 1u);
     }
-    const uint32_t key = keys_sorted[i];
+    const uint32_t key = keys_sorted[i] & key_mask;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
     const uint32_t c = morton_to_linear_checked(g, key);
     if (c == kEmptyCell) {
         atomicOr(err, 2u);
         return;
     }
-    if (i == 0 || keys_sorted[i - 1] != key) {
+    const uint32_t prev = i > 0 ? keys_sorted[i - 1] & key_mask : 0u;
+    if (i == 0 || prev != key) {
         cw[2 * c] = i;
         if (i > 0) {
-            const uint32_t cp = morton_to_linear_checked(g, keys_sorted[i - 1]);
+            const uint32_t cp = morton_to_linear_checked(g, prev);
             if (cp != kEmptyCell) cw[2 * cp + 1] = i;
         }
     }
