@@ -1,4 +1,4 @@
-// scan.cu -- reduce-then-scan exclusive prefix sum (see scan.cuh).
+// scan.cu -- reduce-then-scan exclusive prefix sums, several arrays per launch (see scan.cuh).
 #include "scan.cuh"
 
 namespace sph {
@@ -35,28 +35,48 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) tile_sums_kernel(const uint32_t* __restrict__ in,
-                                                                 uint32_t n,
-                                                                 uint32_t* __restrict__ sums) {
-    __shared__ uint32_t s_warp[33];
-    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    uint32_t t = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) t += in[base + k];
-    uint32_t tot;
-    block_excl_scan(t, s_warp, &tot);
-    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+// ---- batched form: segment k owns tiles [tile0[k], tile0[k + 1]) and tile
+// sums scratch[sums0[k] ...] (tiles + 1 words) ----
+struct ScanBatch {
+    ScanSeg seg[kScanMaxSegs];
+    uint32_t tile0[kScanMaxSegs + 1];
+    uint32_t sums0[kScanMaxSegs];
+    int count;
+};
+
+__device__ __forceinline__ int batch_segment(const ScanBatch& b, uint32_t tile) {
+    int k = 0;
+    while (k + 1 < b.count && tile >= b.tile0[k + 1]) ++k;
+    return k;
 }
 
-// Exclusive scan of the tile sums in place (one block, any count up to
-// kScanThreads * 64), total written to sums[count] and *total.
-__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(uint32_t* sums, uint32_t count,
-                                                                 uint32_t* total) {
+__global__ void __launch_bounds__(kScanThreads) tile_sums_batch_kernel(ScanBatch b,
+                                                                       uint32_t* __restrict__ scratch) {
     __shared__ uint32_t s_warp[33];
+    const int k = batch_segment(b, blockIdx.x);
+    const uint32_t tile = blockIdx.x - b.tile0[k];
+    const uint32_t* __restrict__ in = b.seg[k].in;
+    const uint32_t n = b.seg[k].n;
+    const uint32_t base = tile * kScanTile + threadIdx.x * kScanItems;
+    uint32_t t = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q)
+        if (base + q < n) t += in[base + q];
+    uint32_t tot;
+    block_excl_scan(t, s_warp, &tot);
+    if (threadIdx.x == 0) scratch[b.sums0[k] + tile] = tot;
+}
+
+// One block per segment: its tile sums, scanned in place, and its total.
+__global__ void __launch_bounds__(kScanThreads) scan_sums_batch_kernel(ScanBatch b,
+                                                                       uint32_t* scratch) {
+    __shared__ uint32_t s_warp[33];
+    const int k = blockIdx.x;
+    uint32_t* sums = scratch + b.sums0[k];
+    const uint32_t count = b.tile0[k + 1] - b.tile0[k];
     uint32_t carry = 0;
-    for (uint32_t b = 0; b < count; b += kScanThreads) {
-        const uint32_t i = b + threadIdx.x;
+    for (uint32_t q = 0; q < count; q += kScanThreads) {
+        const uint32_t i = q + threadIdx.x;
         const uint32_t v = i < count ? sums[i] : 0u;
         uint32_t tot;
         const uint32_t e = block_excl_scan(v, s_warp, &tot);
@@ -65,44 +85,55 @@ __global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(uint32_t* sums,
     }
     if (threadIdx.x == 0) {
         sums[count] = carry;
-        if (total) *total = carry;
+        *b.seg[k].total = carry;
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const uint32_t* in,
-                                                                  uint32_t* out, uint32_t n,
-                                                                  const uint32_t* __restrict__ sums) {
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_batch_kernel(
+    ScanBatch b, const uint32_t* __restrict__ scratch) {
     __shared__ uint32_t s_warp[33];
-    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int k = batch_segment(b, blockIdx.x);
+    const uint32_t tile = blockIdx.x - b.tile0[k];
+    const uint32_t* in = b.seg[k].in;
+    uint32_t* out = b.seg[k].out;
+    const uint32_t n = b.seg[k].n;
+    const uint32_t base = tile * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t t = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? in[base + k] : 0u;
-        t += v[k];
+    for (int q = 0; q < kScanItems; ++q) {
+        v[q] = base + q < n ? in[base + q] : 0u;
+        t += v[q];
     }
     uint32_t tot;
-    uint32_t run = sums[blockIdx.x] + block_excl_scan(t, s_warp, &tot);
+    uint32_t run = scratch[b.sums0[k] + tile] + block_excl_scan(t, s_warp, &tot);
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) {
-            out[base + k] = run;
-            run += v[k];
+    for (int q = 0; q < kScanItems; ++q)
+        if (base + q < n) {
+            out[base + q] = run;
+            run += v[q];
         }
 }
 
 }  // namespace
 
-void scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
-                    uint32_t* total, cudaStream_t st) {
-    if (n == 0) {
-        if (total) cudaMemsetAsync(total, 0, 4, st);
-        return;
+void scan_exclusive_batch(const ScanSeg* segs, int count, uint32_t* scratch, cudaStream_t st) {
+    if (count <= 0) return;
+    ScanBatch b;
+    b.count = count < kScanMaxSegs ? count : kScanMaxSegs;
+    uint32_t tiles = 0, words = 0;
+    for (int k = 0; k < b.count; ++k) {
+        b.seg[k] = segs[k];
+        b.tile0[k] = tiles;
+        b.sums0[k] = words;
+        const uint32_t t = (segs[k].n + kScanTile - 1) / kScanTile;
+        tiles += t;
+        words += t + 1;
     }
-    const uint32_t tiles = (n + kScanTile - 1) / kScanTile;
-    tile_sums_kernel<<<tiles, kScanThreads, 0, st>>>(in, n, scratch);
-    scan_sums_kernel<<<1, kScanThreads, 0, st>>>(scratch, tiles, total);
-    scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(in, out, n, scratch);
+    b.tile0[b.count] = tiles;
+    if (tiles) tile_sums_batch_kernel<<<tiles, kScanThreads, 0, st>>>(b, scratch);
+    scan_sums_batch_kernel<<<b.count, kScanThreads, 0, st>>>(b, scratch);
+    if (tiles) scan_tiles_batch_kernel<<<tiles, kScanThreads, 0, st>>>(b, scratch);
 }
 
 }  // namespace sph

@@ -303,13 +303,12 @@ int ts_step(sph_solver2* s, float dt) {
     Pop &L = s->pop[0], &H = s->pop[1];
     const uint32_t gb = s->group_base;
     ts_front(s, dt, false, 0, nullptr, nullptr, nullptr, nullptr);
-    // compaction (prefix sums over keep / split / merge flags)
-    if (H.n) scan_exclusive(H.keep, H.off, H.n, s->scan_scratch, s->tot + 0, st);
-    if (L.n) {
-        scan_exclusive(L.keep, L.off, L.n, s->scan_scratch, s->tot + 1, st);
-        scan_exclusive(L.split, L.soff, L.n, s->scan_scratch, s->tot + 2, st);
-    }
-    scan_exclusive(s->gmerge, s->moff, gb, s->scan_scratch, s->tot + 3, st);
+    // compaction: the prefix sums over keep / split / merge flags, in one batch
+    const ScanSeg segs[4] = {{H.keep, H.off, H.n, s->tot + 0},
+                             {L.keep, L.off, L.n, s->tot + 1},
+                             {L.split, L.soff, L.n, s->tot + 2},
+                             {s->gmerge, s->moff, gb, s->tot + 3}};
+    scan_exclusive_batch(segs, 4, s->scan_scratch, st);
     ts_totals_kernel<<<1, 1, 0, st>>>(s->tot, H.n, L.n, H.cap, L.cap, s->cap_groups, s->ctl, s->err);
     if (H.n)
         ts_compact_kernel<<<blocks_for(H.n), 256, 0, st>>>(outputs(H, nullptr, nullptr), H.off, H.n,
@@ -426,7 +425,10 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
     TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
     s->owned.push_back(s->sort_mem);
     s->sort = sort_scratch_from(s->sort_mem, nmax);
-    TRY(dalloc(&s->scan_scratch, scan_scratch_words(std::max<uint32_t>(nmax, s->cap_groups)), s->owned));
+    TRY(dalloc(&s->scan_scratch,
+               scan_scratch_words((uint32_t)capH) + 2 * scan_scratch_words((uint32_t)capL) +
+                   scan_scratch_words(s->cap_groups),
+               s->owned));
     TRY(dalloc(&s->tot, 4, s->owned));
     TRY(dalloc(&s->gsum, s->cap_groups, s->owned));
     TRY(dalloc(&s->gready, s->cap_groups, s->owned));
