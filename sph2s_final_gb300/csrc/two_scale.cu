@@ -310,20 +310,15 @@ int ts_step(sph_solver2* s, float dt) {
                              {s->gmerge, s->moff, gb, s->tot + 3}};
     scan_exclusive_batch(segs, 4, s->scan_scratch, st);
     ts_totals_kernel<<<1, 1, 0, st>>>(s->tot, H.n, L.n, H.cap, L.cap, s->cap_groups, s->ctl, s->err);
-    if (H.n)
-        ts_compact_kernel<<<blocks_for(H.n), 256, 0, st>>>(outputs(H, nullptr, nullptr), H.off, H.n,
-                                                           H.cap, H.pos, H.vel, H.stt, H.grp);
-    if (L.n) {
-        ts_compact_kernel<<<blocks_for(L.n), 256, 0, st>>>(outputs(L, nullptr, nullptr), L.off, L.n,
-                                                           L.cap, L.pos, L.vel, L.stt, L.grp);
-        ts_children_kernel<<<blocks_for(L.n), 256, 0, st>>>(
-            outputs(L, nullptr, nullptr), L.soff, L.rho, L.n, s->P.mass[0], s->ctl, H.cap, H.pos,
-            H.vel, H.stt, H.grp);
+    {
+        const TSState hs = {H.pos, H.vel, H.stt, H.grp, H.cap};
+        const TSState ls = {L.pos, L.vel, L.stt, L.grp, L.cap};
+        const uint32_t work = H.n + L.n + gb;
+        if (work)
+            ts_finish_kernel<<<blocks_for(work), 256, 0, st>>>(
+                outputs(H, nullptr, nullptr), H.off, H.n, outputs(L, nullptr, nullptr), L.off,
+                L.soff, L.rho, L.n, s->P.mass[0], s->gmerge, s->moff, s->gacc, gb, s->ctl, hs, ls);
     }
-    if (gb)
-        ts_merge_spawn_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gmerge, s->moff, s->gacc, gb,
-                                                              s->ctl, L.cap, L.pos, L.vel, L.stt,
-                                                              L.grp);
     ts_advance_counters_kernel<<<1, 1, 0, st>>>(s->ctl, s->cap_groups);
     SPH_CUDA(cudaGetLastError());
     SPH_CUDA(cudaMemcpyAsync(s->ctl_host, s->ctl, 4 * kCtlWords, cudaMemcpyDeviceToHost, st));

@@ -569,11 +569,12 @@ static __global__ void ts_totals_kernel(const uint32_t* __restrict__ tot, uint32
 }
 
 // Survivors -> state arrays at their compacted positions.
-static __global__ void __launch_bounds__(256) ts_compact_kernel(
-    const TSOut o, const uint32_t* __restrict__ off, uint32_t n, uint32_t cap, float4* __restrict__ pos,
-    float4* __restrict__ vel, int32_t* __restrict__ stt, uint32_t* __restrict__ grp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !o.keep[i]) return;
+__device__ __forceinline__ void ts_compact_one(uint32_t i, const TSOut& o,
+                                               const uint32_t* __restrict__ off, uint32_t cap,
+                                               float4* __restrict__ pos, float4* __restrict__ vel,
+                                               int32_t* __restrict__ stt,
+                                               uint32_t* __restrict__ grp) {
+    if (!o.keep[i]) return;
     const uint32_t d = off[i];
     if (d >= cap) return;
     pos[d] = o.ipos[i];
@@ -586,13 +587,14 @@ static __global__ void __launch_bounds__(256) ts_compact_kernel(
 // sorted order of their parents (insertHighResParticles,
 // SPH2S_FINAL_TWO_SCALE/Solver.cu:541-586: radius 0.5 (3 m / (4 pi rho))^(1/3),
 // directions (+-1, +-1, +-1)/sqrt(3), parent velocity, lambda 0, state 6).
-static __global__ void __launch_bounds__(256) ts_children_kernel(
-    const TSOut o, const uint32_t* __restrict__ split_off, const float* __restrict__ rho_low,
-    uint32_t n_low, float mass_low, const uint32_t* __restrict__ ctl, uint32_t cap_high,
-    float4* __restrict__ pos_h, float4* __restrict__ vel_h, int32_t* __restrict__ stt_h,
-    uint32_t* __restrict__ grp_h) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_low || !o.split[i]) return;
+__device__ __forceinline__ void ts_children_one(uint32_t i, const TSOut& o,
+                                                const uint32_t* __restrict__ split_off,
+                                                const float* __restrict__ rho_low, float mass_low,
+                                                const uint32_t* __restrict__ ctl, uint32_t cap_high,
+                                                float4* __restrict__ pos_h, float4* __restrict__ vel_h,
+                                                int32_t* __restrict__ stt_h,
+                                                uint32_t* __restrict__ grp_h) {
+    if (!o.split[i]) return;
     const uint32_t q = split_off[i];
     const uint32_t base = ctl[kCtlSurvH] + 8u * q;
     const float4 x = o.ipos[i], v = o.ivel[i];
@@ -612,13 +614,12 @@ static __global__ void __launch_bounds__(256) ts_children_kernel(
 }
 
 // One LOW particle per merged group, after the LOW survivors, by group id.
-static __global__ void __launch_bounds__(256) ts_merge_spawn_kernel(
-    const uint32_t* __restrict__ gmerge, const uint32_t* __restrict__ merge_off,
-    const unsigned long long* __restrict__ gacc, uint32_t group_base,
-    const uint32_t* __restrict__ ctl, uint32_t cap_low, float4* __restrict__ pos_l,
-    float4* __restrict__ vel_l, int32_t* __restrict__ stt_l, uint32_t* __restrict__ grp_l) {
-    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gi >= group_base || !gmerge[gi]) return;
+__device__ __forceinline__ void ts_merge_spawn_one(
+    uint32_t gi, const uint32_t* __restrict__ gmerge, const uint32_t* __restrict__ merge_off,
+    const unsigned long long* __restrict__ gacc, const uint32_t* __restrict__ ctl,
+    uint32_t cap_low, float4* __restrict__ pos_l, float4* __restrict__ vel_l,
+    int32_t* __restrict__ stt_l, uint32_t* __restrict__ grp_l) {
+    if (!gmerge[gi]) return;
     const uint32_t m = merge_off[gi];
     const uint32_t dst = ctl[kCtlSurvL] + m;
     if (dst >= cap_low) return;
@@ -631,6 +632,42 @@ static __global__ void __launch_bounds__(256) ts_merge_spawn_kernel(
     vel_l[dst] = make_float4(f[3], f[4], f[5], 0.0f);
     stt_l[dst] = 2;
     grp_l[dst] = kNoGroup;
+}
+
+// The next step's state arrays of one population.
+struct TSState {
+    float4* pos;
+    float4* vel;
+    int32_t* stt;
+    uint32_t* grp;
+    uint32_t cap;
+};
+
+// Everything that builds the next state after the prefix sums, in one launch
+// over [HIGH particles | LOW particles | groups]: survivors to their compacted
+// slots, the split children after the HIGH survivors, merged particles after
+// the LOW survivors.
+static __global__ void __launch_bounds__(256) ts_finish_kernel(
+    const TSOut oh, const uint32_t* __restrict__ off_h, uint32_t n_h, const TSOut ol,
+    const uint32_t* __restrict__ off_l, const uint32_t* __restrict__ split_off,
+    const float* __restrict__ rho_l, uint32_t n_l, float mass_low,
+    const uint32_t* __restrict__ gmerge, const uint32_t* __restrict__ merge_off,
+    const unsigned long long* __restrict__ gacc, uint32_t n_groups,
+    const uint32_t* __restrict__ ctl, TSState H, TSState L) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_h) {
+        ts_compact_one(i, oh, off_h, H.cap, H.pos, H.vel, H.stt, H.grp);
+        return;
+    }
+    i -= n_h;
+    if (i < n_l) {
+        ts_compact_one(i, ol, off_l, L.cap, L.pos, L.vel, L.stt, L.grp);
+        ts_children_one(i, ol, split_off, rho_l, mass_low, ctl, H.cap, H.pos, H.vel, H.stt, H.grp);
+        return;
+    }
+    i -= n_l;
+    if (i < n_groups)
+        ts_merge_spawn_one(i, gmerge, merge_off, gacc, ctl, L.cap, L.pos, L.vel, L.stt, L.grp);
 }
 
 // Advances the persistent counters after the step; the group count saturates
