@@ -138,7 +138,7 @@ __device__ __forceinline__ void force_one(
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256) force_kernel(
+__global__ void __launch_bounds__(256, 6) force_kernel(
     const float4* __restrict__ pos, const float4* __restrict__ xa, const float4* __restrict__ va,
     const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
