@@ -173,6 +173,7 @@ __device__ __forceinline__ float adj_force_one(
                                           cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz));
         if (__ldg(&bnear[home])) {
             const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+            const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
             for (int cz = s.z0; cz <= s.z1; ++cz)
                 for (int cy = s.y0; cy <= s.y1; ++cy) {
                     const uint32_t row = linear_cell(P.g, 0, cy, cz);
@@ -181,6 +182,7 @@ __device__ __forceinline__ float adj_force_one(
                         const uint32_t e = min(r.y, nb);
                         for (uint32_t k = r.x; k < e; ++k) {
                             const float4 xk = __ldg(&bpos[k]);
+                            if (xk.w >= reach) break;  // the rest of the cell lies deeper
                             float dx, dy, dz;
                             const float r2 = dist2(xi.x, xi.y, xi.z, xk.x, xk.y, xk.z, dx, dy, dz);
                             if (r2 < P.T) {

@@ -257,11 +257,11 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
                 hv[R.p_off + i] = v ? make_float4(v[0], v[1], v[2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             for (uint32_t i = 0; i < d.n_boundary; ++i) {
-                float w;
-                std::memcpy(&w, &i, 4);
                 const float* x = d.boundary_xyz + 3 * (size_t)i;
-                hb[R.b_off + i] = make_float4(x[0], x[1], x[2], w);
+                hb[R.b_off + i] = make_float4(x[0], x[1], x[2], 0.0f);
             }
+            // boundary_reach's scan order, as the single-scene solver's
+            boundary_by_depth(R.P.g, hb.data() + R.b_off, d.n_boundary);
         }
         TRY(dalloc(&b->pos0, b->N, b->owned));
         if (b->N) {

@@ -21,6 +21,7 @@ struct GridParams {
     int dx, dy, dz;     // Grid::Dimensions
     float spacing;      // Grid::Spacing
     int mbits;          // Morton bits per axis: ceil(log2(max dim))
+    float ex, ey, ez;   // far corner of the grid's box, origin + dims * spacing
 };
 
 // Per-solver constants, passed by value to every kernel (the reference keeps
@@ -40,6 +41,7 @@ struct SimParams {
     float bnd_coef;   // 0.02 c^2 * m_b / (m + m_b)
     float two_over_h; // 2 / h
     float gravity;    // -9.81 along y
+    float bmargin;    // rounding allowance of the boundary scan's depth cut (boundary_reach)
 };
 
 // computeCoordinates(Off), SPH2S_FINAL_SINGLE_SCALE/Solver.cu:20-57.  The
@@ -128,6 +130,24 @@ __device__ __forceinline__ Stencil stencil(const GridParams& g, float x, float y
     s.z0 = cell_coord_off(z, -h, g.oz, g.spacing, g.dz);
     s.z1 = cell_coord_off(z, h, g.oz, g.spacing, g.dz);
     return s;
+}
+
+// Boundary particles are stored, within each cell, by increasing depth
+// outside the grid's box (float4 w, the largest per-axis distance outside,
+// rounded down: a lower bound on the distance to the box).  The clamped cell
+// assignment (Solver.cu:35-37) puts every layer of the reference's boundary
+// shell that lies outside the grid into the edge cells, up to five layers on
+// each clamped axis.  A boundary particle j within h of a particle at x
+// satisfies depth_j <= |x_j - x| + dist(x, box) < h + dist(x, box), so a cell
+// scan may stop at the first particle deeper than the returned reach: the
+// neighbour set is that of the full scan.  dist(x, box) is bounded above by
+// the sum of the per-axis distances outside; bmargin covers the rounding.
+__device__ __forceinline__ float boundary_reach(const GridParams& g, float h, float bmargin,
+                                                float x, float y, float z) {
+    const float ox = fmaxf(fmaxf(__fsub_rn(g.ox, x), __fsub_rn(x, g.ex)), 0.0f);
+    const float oy = fmaxf(fmaxf(__fsub_rn(g.oy, y), __fsub_rn(y, g.ey)), 0.0f);
+    const float oz = fmaxf(fmaxf(__fsub_rn(g.oz, z), __fsub_rn(z, g.ez)), 0.0f);
+    return h + ox + oy + oz + bmargin;
 }
 
 // Boundary weight shape of evaluateBoundaryWeight (Solver.cu:169-196)

@@ -97,6 +97,7 @@ __device__ __forceinline__ void force_one(
                                       cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz));
     if (__ldg(&bnear[home])) {
         const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+        const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
         for (int cz = s.z0; cz <= s.z1; ++cz)
             for (int cy = s.y0; cy <= s.y1; ++cy) {
                 const uint32_t row = linear_cell(P.g, 0, cy, cz);
@@ -105,6 +106,7 @@ __device__ __forceinline__ void force_one(
                     const uint32_t e = min(r.y, nb);
                     for (uint32_t j = r.x; j < e; ++j) {
                         const float4 xj = __ldg(&bpos[j]);
+                        if (xj.w >= reach) break;  // the rest of the cell lies deeper
                         float dx, dy, dz;
                         float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
                         if (r2 < P.T) {

@@ -4,8 +4,11 @@
 // 45/(pi h^6), boundary 0.02 c^2 / r); they are evaluated in double and
 // rounded once to float.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <string>
+#include <utility>
+#include <vector>
 #include "common.cuh"
 #include "errors.h"
 
@@ -49,7 +52,44 @@ inline GridParams make_grid_params(const sph_grid& g) {
     p.dz = g.dims[2];
     p.spacing = g.spacing;
     p.mbits = morton_bits_for(g);
+    p.ex = (float)((double)g.origin[0] + (double)g.dims[0] * (double)g.spacing);
+    p.ey = (float)((double)g.origin[1] + (double)g.dims[1] * (double)g.spacing);
+    p.ez = (float)((double)g.origin[2] + (double)g.dims[2] * (double)g.spacing);
     return p;
+}
+
+// Rounding allowance of the boundary depth cut (boundary_reach): 1e-3 h plus
+// a few ulps of the box's coordinates.
+inline float boundary_margin(const GridParams& p, float h) {
+    double m = 0.0;
+    for (float v : {p.ox, p.oy, p.oz, p.ex, p.ey, p.ez}) m = std::max(m, std::fabs((double)v));
+    return (float)(1e-3 * (double)h + 32.0 * std::ldexp(1.0, -24) * (m + (double)h));
+}
+
+// Orders boundary particles (float4, w free) by increasing depth outside the
+// grid's box, stably, and stores the depth, rounded down to float, in w; the
+// device sort by cell keeps this order within each cell (boundary_reach).
+inline void boundary_by_depth(const GridParams& p, float4* hb, uint32_t n) {
+    std::vector<std::pair<double, uint32_t>> d(n);
+    const double lo[3] = {p.ox, p.oy, p.oz}, hi[3] = {p.ex, p.ey, p.ez};
+    for (uint32_t i = 0; i < n; ++i) {
+        const double x[3] = {hb[i].x, hb[i].y, hb[i].z};
+        double m = 0.0;
+        for (int a = 0; a < 3; ++a) m = std::max(m, std::max(lo[a] - x[a], x[a] - hi[a]));
+        d[i] = {m, i};
+    }
+    std::stable_sort(d.begin(), d.end(),
+                     [](const std::pair<double, uint32_t>& a, const std::pair<double, uint32_t>& b) {
+                         return a.first < b.first;
+                     });
+    std::vector<float4> out(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        float w = (float)d[k].first;
+        if ((double)w > d[k].first) w = std::nextafter(w, 0.0f);
+        out[k] = hb[d[k].second];
+        out[k].w = w;
+    }
+    std::copy(out.begin(), out.end(), hb);
 }
 
 inline int make_sim_params(const sph_config& c, SimParams* out) {
@@ -80,6 +120,7 @@ inline int make_sim_params(const sph_config& c, SimParams* out) {
     P.bnd_coef = (float)(0.02 * (double)c.speed_sound * c.speed_sound * mb / (m + mb));
     P.two_over_h = (float)(2.0 / hd);
     P.gravity = -9.81f;
+    P.bmargin = boundary_margin(P.g, h);
     *out = P;
     return SPH_OK;
 }

@@ -279,6 +279,8 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
         std::memcpy(&w, &i, 4);
         hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
     }
+    // boundary_reach's scan order: by depth outside the grid's box within each cell
+    boundary_by_depth(make_grid_params(config->grid), hb.data(), n_boundary);
     return sph_ss::create_solver(config, hp.data(), hv.data(), hp.data(), n_fluid, hb.data(),
                                  n_boundary, 0, out);
 }

@@ -6,7 +6,8 @@
 //   float4 pos[n]   positions in the sorted order of the last step, persistent id in w
 //   float4 vel[n]   velocities, same order
 //   float4 pos0[n]  positions at creation, creation order (rollout restarts)
-//   float4 bpos[nb] boundary positions, presorted on the fluid grid, input index in w
+//   float4 bpos[nb] boundary positions, presorted on the fluid grid, depth outside the
+//                   grid's box in w (the order boundary_reach's cut relies on)
 // The next step's sort is stable with respect to the stored order, which is
 // why the order itself is part of the state.  Re-presorting the stored
 // (already sorted) boundary reproduces it exactly.

@@ -145,6 +145,7 @@ int make_ts_params(const sph_config2& c, TSParams* out) {
     P.hi = c.refine_hi;
     P.lo43 = std::llrint((double)c.refine_lo * 8796093022208.0);
     P.hi43 = std::llrint((double)c.refine_hi * 8796093022208.0);
+    P.bmargin = boundary_margin(P.g[0], P.h[0]);
     *out = P;
     return SPH_OK;
 }
@@ -377,8 +378,8 @@ int upload_pop(sph_solver2* s, int r, const HostPop& h) {
 }
 
 // Allocates a handle for capacities capL / capH, uploads both populations,
-// sets the group and id counters and presorts the boundary (float4, input
-// index in w) on the LOW grid.
+// sets the group and id counters and presorts the boundary (float4, ordered
+// by depth outside the LOW grid's box with the depth in w) on the LOW grid.
 int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, uint64_t capH,
                    const HostPop* pops, const float4* hb, uint32_t n_boundary,
                    uint32_t group_base, const uint32_t next_id[2], uint64_t step,
@@ -554,6 +555,7 @@ int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
         std::memcpy(&w, &i, 4);
         hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
     }
+    boundary_by_depth(P.g[0], hb.data(), n_boundary);  // boundary_reach's scan order
     const uint32_t next_id[2] = {n_low, n_high};
     return create_solver2(config, P, capL, capH, pops, hb.data(), n_boundary, 0, next_id, 0, out);
 }

@@ -41,6 +41,7 @@ struct TSParams {
     int coupled;              // fixed populations: unit weights, no clamp, no state changes
     int surface;              // surface trigger: split / merge by rho < surf_rho
     float surf_rho;
+    float bmargin;            // rounding allowance of the boundary depth cut (boundary_reach)
 };
 
 // Mexican hat wavelet of the colour output (evaluateMexicanHat3D,
@@ -452,6 +453,7 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
                                        cell_coord(xi.z, P.g[0].oz, P.g[0].spacing, P.g[0].dz));
     if (__ldg(&bnear[bhome])) {
         const Stencil st = stencil(P.g[0], xi.x, xi.y, xi.z, P.h[0]);
+        const float reach = boundary_reach(P.g[0], P.h[0], P.bmargin, xi.x, xi.y, xi.z);
         for (int cz = st.z0; cz <= st.z1; ++cz)
             for (int cy = st.y0; cy <= st.y1; ++cy) {
                 const uint32_t row = linear_cell(P.g[0], 0, cy, cz);
@@ -460,6 +462,7 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
                     const uint32_t e = min(r.y, nb);
                     for (uint32_t j = r.x; j < e; ++j) {
                         const float4 xj = __ldg(&bpos[j]);
+                        if (xj.w >= reach) break;  // the rest of the cell lies deeper
                         float dx, dy, dz;
                         const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
                         if (r2 < P.T[0]) {
