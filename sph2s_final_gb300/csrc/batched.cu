@@ -260,8 +260,6 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
                 const float* x = d.boundary_xyz + 3 * (size_t)i;
                 hb[R.b_off + i] = make_float4(x[0], x[1], x[2], 0.0f);
             }
-            // boundary_reach's scan order, as the single-scene solver's
-            boundary_by_depth(R.P.g, hb.data() + R.b_off, d.n_boundary);
         }
         TRY(dalloc(&b->pos0, b->N, b->owned));
         if (b->N) {
@@ -275,16 +273,25 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
             float4* braw = nullptr;
             TRY(dalloc(&braw, b->NB, b->owned));
             TRY(check_cuda(cudaMemcpy(braw, hb.data(), 16 * (size_t)b->NB, cudaMemcpyHostToDevice), "upload", __FILE__, __LINE__));
+            // keys (scene, cell, depth class): each cell's boundary particles by
+            // non-decreasing depth, the order boundary_reach's cut needs; the
+            // class bits are those every scene allows
+            int sbits = 1;
+            while ((1u << sbits) < num_scenes) ++sbits;
+            int qb = 8;
+            for (const SceneRec& R : b->recs_h)
+                qb = std::min(qb, boundary_depth_bits(R.P.g, R.P.h, b->shift + sbits));
+            const int bpasses = sort_passes(b->shift + sbits + qb);
             sort_reset(b->sort, b->stream);
-            b_hash_hist_kernel<256><<<pgrid(b, b->nbtiles), 256, 0, b->stream>>>(
-                b->btiles, b->nbtiles, b->recs, braw, b->shift, b->passes, true, b->keys[0],
+            b_boundary_hash_hist_kernel<256><<<pgrid(b, b->nbtiles), 256, 0, b->stream>>>(
+                b->btiles, b->nbtiles, b->recs, braw, b->shift, qb, bpasses, b->keys[0],
                 b->sort.hist);
-            sort_scan(b->passes, b->sort, b->stream);
-            const int o = sort_passes_run(b->keys, b->vals, nullptr, b->NB, b->passes, b->sort,
+            sort_scan(bpasses, b->sort, b->stream);
+            const int o = sort_passes_run(b->keys, b->vals, nullptr, b->NB, bpasses, b->sort,
                                           b->err, 0, b->stream);
             b_gather_cells_kernel<256, false><<<pgrid(b, b->nbtiles), 256, 0, b->stream>>>(
                 b->btiles, b->nbtiles, b->recs, b->keys[o], b->vals[o], b->NB, b->shift, true, braw,
-                nullptr, b->bpos, nullptr, b->bcells, b->err);
+                nullptr, b->bpos, nullptr, b->bcells, b->err, qb);
             TRY(check_cuda(cudaStreamSynchronize(b->stream), "boundary presort", __FILE__, __LINE__));
             cudaFree(braw);
             b->owned.pop_back();

@@ -56,14 +56,47 @@ __global__ void __launch_bounds__(BS) b_hash_hist_kernel(const uint2* __restrict
     }
 }
 
+// Boundary presort keys of a batch: (scene, cell) above qb bits of depth
+// class (depth_class, quantum = h/16 of the scene); w becomes the class's
+// lower bound, as in the single-scene presort.
+template <int BS>
+__global__ void __launch_bounds__(BS) b_boundary_hash_hist_kernel(
+    const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
+    float4* __restrict__ b, int shift, int qb, int passes, uint32_t* __restrict__ keys,
+    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kSortMaxPasses][256];
+    for (int i = threadIdx.x; i < kSortMaxPasses * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
+        const uint2 tile = tiles[t];
+        const SceneRec& R = recs[tile.x];
+        const uint32_t i = tile.y + threadIdx.x;
+        if (i < R.b_off + R.b_n) {
+            float4 p = b[i];
+            const DepthClass dc = depth_class(R.P.g, p.x, p.y, p.z, R.P.h / 16.0f, qb);
+            const uint32_t k = (((tile.x << shift) | cell_key(R.P.g, p.x, p.y, p.z)) << qb) | dc.cls;
+            p.w = dc.lb;
+            b[i] = p;
+            keys[i] = k;
+            sort_hist_add(sh, k, passes);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
 // Reorder + per-scene cell ranges; indices stored in the tables are global.
+// Keys are shifted right by key_shift first (the boundary presort's depth bits).
 template <int BS, bool WITH_VEL>
 __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     int shift, bool boundary, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ err, int key_shift = 0) {
     const uint32_t lmask = (1u << shift) - 1u;
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
@@ -79,7 +112,7 @@ __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
         }
         pos_out[i] = pos_in[q];
         if (WITH_VEL) vel_out[i] = vel_in[q];
-        const uint32_t key = keys_sorted[i];
+        const uint32_t key = keys_sorted[i] >> key_shift;
         uint32_t* cw = reinterpret_cast<uint32_t*>(cells + R.c_off);
         const uint32_t c = (key >> shift) == tile.x ? morton_to_linear_checked(R.P.g, key & lmask)
                                                     : kEmptyCell;
@@ -87,10 +120,11 @@ __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
             atomicOr(err, 2u);
             continue;
         }
-        if (i == beg || keys_sorted[i - 1] != key) {
+        const uint32_t prev = i > beg ? keys_sorted[i - 1] >> key_shift : 0u;
+        if (i == beg || prev != key) {
             cw[2 * c] = i;
             if (i > beg) {
-                const uint32_t cp = morton_to_linear_checked(R.P.g, keys_sorted[i - 1] & lmask);
+                const uint32_t cp = morton_to_linear_checked(R.P.g, prev & lmask);
                 if (cp != kEmptyCell) cw[2 * cp + 1] = i;
             }
         }

@@ -18,7 +18,7 @@ using sph::SortScratch;
 struct sph_batch {
     uint32_t S = 0;                  // scenes
     uint32_t N = 0, NB = 0, NC = 0;  // fluid, boundary, cells (all scenes)
-    int shift = 0, passes = 0, bpasses = 0;
+    int shift = 0, passes = 0;
     std::vector<SceneRec> recs_h;
     SceneRec* recs = nullptr;
     cudaStream_t stream = nullptr;

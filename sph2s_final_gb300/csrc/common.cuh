@@ -132,9 +132,9 @@ __device__ __forceinline__ Stencil stencil(const GridParams& g, float x, float y
     return s;
 }
 
-// Boundary particles are stored, within each cell, by increasing depth
-// outside the grid's box (float4 w, the largest per-axis distance outside,
-// rounded down: a lower bound on the distance to the box).  The clamped cell
+// Boundary particles are stored, within each cell, by non-decreasing w, a
+// lower bound on their depth outside the grid's box (depth_class: the largest
+// per-axis distance outside, quantised down).  The clamped cell
 // assignment (Solver.cu:35-37) puts every layer of the reference's boundary
 // shell that lies outside the grid into the edge cells, up to five layers on
 // each clamped axis.  A boundary particle j within h of a particle at x
@@ -148,6 +148,26 @@ __device__ __forceinline__ float boundary_reach(const GridParams& g, float h, fl
     const float oy = fmaxf(fmaxf(__fsub_rn(g.oy, y), __fsub_rn(y, g.ey)), 0.0f);
     const float oz = fmaxf(fmaxf(__fsub_rn(g.oz, z), __fsub_rn(z, g.ez)), 0.0f);
     return h + ox + oy + oz + bmargin;
+}
+
+// Depth class of a boundary particle for its presort key (qb low bits below
+// the cell key; qb = 0 disables the cut) and the class's lower bound, which
+// becomes the particle's w.  The class is one below floor(depth / quantum) so
+// that the bound stays below the exact depth whatever the rounding of the
+// computed one (quantum is far above the coordinates' ulp).
+struct DepthClass {
+    uint32_t cls;
+    float lb;
+};
+__device__ __forceinline__ DepthClass depth_class(const GridParams& g, float x, float y, float z,
+                                                  float quantum, int qb) {
+    if (qb <= 0) return {0u, 0.0f};
+    float d = fmaxf(fmaxf(__fsub_rn(g.ox, x), __fsub_rn(x, g.ex)), 0.0f);
+    d = fmaxf(d, fmaxf(__fsub_rn(g.oy, y), __fsub_rn(y, g.ey)));
+    d = fmaxf(d, fmaxf(__fsub_rn(g.oz, z), __fsub_rn(z, g.ez)));
+    float c = floorf(__fdiv_rn(d, quantum)) - 1.0f;
+    c = fminf(fmaxf(c, 0.0f), (float)((1u << qb) - 1u));
+    return {(uint32_t)c, __fmul_rn(c, quantum)};
 }
 
 // Boundary weight shape of evaluateBoundaryWeight (Solver.cu:169-196)

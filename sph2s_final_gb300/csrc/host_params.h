@@ -7,8 +7,6 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
-#include <utility>
-#include <vector>
 #include "common.cuh"
 #include "errors.h"
 
@@ -66,30 +64,15 @@ inline float boundary_margin(const GridParams& p, float h) {
     return (float)(1e-3 * (double)h + 32.0 * std::ldexp(1.0, -24) * (m + (double)h));
 }
 
-// Orders boundary particles (float4, w free) by increasing depth outside the
-// grid's box, stably, and stores the depth, rounded down to float, in w; the
-// device sort by cell keeps this order within each cell (boundary_reach).
-inline void boundary_by_depth(const GridParams& p, float4* hb, uint32_t n) {
-    std::vector<std::pair<double, uint32_t>> d(n);
-    const double lo[3] = {p.ox, p.oy, p.oz}, hi[3] = {p.ex, p.ey, p.ez};
-    for (uint32_t i = 0; i < n; ++i) {
-        const double x[3] = {hb[i].x, hb[i].y, hb[i].z};
-        double m = 0.0;
-        for (int a = 0; a < 3; ++a) m = std::max(m, std::max(lo[a] - x[a], x[a] - hi[a]));
-        d[i] = {m, i};
-    }
-    std::stable_sort(d.begin(), d.end(),
-                     [](const std::pair<double, uint32_t>& a, const std::pair<double, uint32_t>& b) {
-                         return a.first < b.first;
-                     });
-    std::vector<float4> out(n);
-    for (uint32_t k = 0; k < n; ++k) {
-        float w = (float)d[k].first;
-        if ((double)w > d[k].first) w = std::nextafter(w, 0.0f);
-        out[k] = hb[d[k].second];
-        out[k].w = w;
-    }
-    std::copy(out.begin(), out.end(), hb);
+// Depth classes of the boundary presort (depth_class): quantum h/16, and as
+// many key bits as the cell key leaves free, at most 8; 0 (no cut) when the
+// quantum is not far above the coordinates' rounding.
+inline float boundary_quantum(float h) { return h / 16.0f; }
+inline int boundary_depth_bits(const GridParams& p, float h, int key_bits) {
+    double m = 0.0;
+    for (float v : {p.ox, p.oy, p.oz, p.ex, p.ey, p.ez}) m = std::max(m, std::fabs((double)v));
+    if ((double)boundary_quantum(h) < std::ldexp(m + (double)h, -16)) return 0;
+    return std::max(0, std::min(8, 32 - key_bits));
 }
 
 inline int make_sim_params(const sph_config& c, SimParams* out) {

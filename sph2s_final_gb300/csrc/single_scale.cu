@@ -206,15 +206,19 @@ int create_solver(const sph_config* config, const float4* hpos, const float4* hv
             TRY(dalloc(&braw, n_boundary));
             cudaError_t e = cudaMemcpyAsync(braw, hbound, sizeof(float4) * n_boundary, cudaMemcpyHostToDevice, s->stream);
             if (e == cudaSuccess) {
-                int passes = sort_passes(s->key_bits);
+                // keys (cell, depth class): each cell's boundary particles by
+                // non-decreasing depth, the order boundary_reach's cut needs
+                const int qb = boundary_depth_bits(s->P.g, s->P.h, s->key_bits);
+                int passes = sort_passes(s->key_bits + qb);
                 sort_reset(s->sort, s->stream);
-                hash_hist_kernel<<<blocks_for(n_boundary) > 1216 ? 1216 : blocks_for(n_boundary), 256, 0, s->stream>>>(
-                    braw, n_boundary, s->P.g, passes, s->keys[0], s->sort.hist);
+                boundary_hash_hist_kernel<<<blocks_for(n_boundary) > 1216 ? 1216 : blocks_for(n_boundary), 256, 0, s->stream>>>(
+                    braw, n_boundary, s->P.g, qb, boundary_quantum(s->P.h), passes, s->keys[0],
+                    s->sort.hist);
                 sort_scan(passes, s->sort, s->stream);
                 int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort, s->err, 0, s->stream);
                 gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
                     s->keys[o], s->vals[o], n_boundary, s->P.g, braw, nullptr, s->bpos, nullptr, s->bcells,
-                    s->err);
+                    s->err, qb);
                 e = cudaGetLastError();
                 if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
             }
@@ -279,8 +283,6 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
         std::memcpy(&w, &i, 4);
         hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
     }
-    // boundary_reach's scan order: by depth outside the grid's box within each cell
-    boundary_by_depth(make_grid_params(config->grid), hb.data(), n_boundary);
     return sph_ss::create_solver(config, hp.data(), hv.data(), hp.data(), n_fluid, hb.data(),
                                  n_boundary, 0, out);
 }

@@ -37,7 +37,33 @@ static __global__ void __launch_bounds__(256) hash_hist_kernel(const float4* __r
     }
 }
 
-// Reorders the state by the sorted permutation and records cell ranges.
+// Boundary presort keys: the cell's Morton key above qb bits of depth class
+// (depth_class), so that the stable sort stores each cell's boundary
+// particles by non-decreasing w; w becomes the class's lower bound.
+static __global__ void __launch_bounds__(256) boundary_hash_hist_kernel(
+    float4* __restrict__ b, uint32_t n, GridParams g, int qb, float quantum, int passes,
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kSortMaxPasses][256];
+    for (int i = threadIdx.x; i < kSortMaxPasses * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 p = b[i];
+        const DepthClass dc = depth_class(g, p.x, p.y, p.z, quantum, qb);
+        const uint32_t k = (cell_key(g, p.x, p.y, p.z) << qb) | dc.cls;
+        p.w = dc.lb;
+        b[i] = p;
+        keys[i] = k;
+        sort_hist_add(sh, k, passes);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// Reorders the state by the sorted permutation and records cell ranges (keys
+// shifted right by key_shift first: the boundary presort's depth bits).
 // Every index read from the sort output is range-checked: if a bounded wait in
 // the sort gave up, its output is garbage, and this kernel then records an
 // error and stays in bounds instead of faulting.
@@ -46,7 +72,7 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     GridParams g, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ err, int key_shift = 0) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t q = perm[i];
@@ -56,17 +82,18 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
     }
     pos_out[i] = pos_in[q];
     if (WITH_VEL) vel_out[i] = vel_in[q];
-    uint32_t key = keys_sorted[i];
+    uint32_t key = keys_sorted[i] >> key_shift;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
     uint32_t c = morton_to_linear_checked(g, key);
     if (c == kEmptyCell) {
         atomicOr(err, 2u);
         return;
     }
-    if (i == 0 || keys_sorted[i - 1] != key) {
+    const uint32_t prev = i > 0 ? keys_sorted[i - 1] >> key_shift : 0u;
+    if (i == 0 || prev != key) {
         cw[2 * c] = i;
         if (i > 0) {
-            uint32_t cp = morton_to_linear_checked(g, keys_sorted[i - 1]);
+            uint32_t cp = morton_to_linear_checked(g, prev);
             if (cp != kEmptyCell) cw[2 * cp + 1] = i;
         }
     }

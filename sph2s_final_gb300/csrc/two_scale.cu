@@ -458,18 +458,21 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
         cudaError_t e = cudaMalloc(&braw, 16 * (size_t)n_boundary);
         if (e == cudaSuccess) e = cudaMemcpy(braw, hb, 16 * (size_t)n_boundary, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) {
-            const int passes = sort_passes(s->pop[0].key_bits);
+            // keys (cell, depth class): the order boundary_reach's cut needs
+            const int qb = boundary_depth_bits(s->P.g[0], s->P.h[0], s->pop[0].key_bits);
+            const int passes = sort_passes(s->pop[0].key_bits + qb);
             sort_reset(s->sort, s->stream);
             uint32_t hbk = blocks_for(n_boundary);
             if (hbk > 1216) hbk = 1216;
-            hash_hist_kernel<<<hbk, 256, 0, s->stream>>>(braw, n_boundary, s->P.g[0], passes,
-                                                         s->keys[0], s->sort.hist);
+            boundary_hash_hist_kernel<<<hbk, 256, 0, s->stream>>>(
+                braw, n_boundary, s->P.g[0], qb, boundary_quantum(s->P.h[0]), passes, s->keys[0],
+                s->sort.hist);
             sort_scan(passes, s->sort, s->stream);
             const int o = sort_passes_run(s->keys, s->vals, nullptr, n_boundary, passes, s->sort,
                                           s->err, 0, s->stream);
             gather_cells_kernel<false><<<blocks_for(n_boundary), 256, 0, s->stream>>>(
                 s->keys[o], s->vals[o], n_boundary, s->P.g[0], braw, nullptr, s->bpos, nullptr,
-                s->bcells, s->err);
+                s->bcells, s->err, qb);
             e = cudaGetLastError();
             if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         }
@@ -555,7 +558,6 @@ int sph2_create(const sph_config2* config, const float* low_xyz, uint32_t n_low,
         std::memcpy(&w, &i, 4);
         hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
     }
-    boundary_by_depth(P.g[0], hb.data(), n_boundary);  // boundary_reach's scan order
     const uint32_t next_id[2] = {n_low, n_high};
     return create_solver2(config, P, capL, capH, pops, hb.data(), n_boundary, 0, next_id, 0, out);
 }
