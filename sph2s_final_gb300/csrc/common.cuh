@@ -133,8 +133,8 @@ __device__ __forceinline__ Stencil stencil(const GridParams& g, float x, float y
 }
 
 // Boundary particles are stored, within each cell, by non-decreasing w, a
-// lower bound on their depth outside the grid's box (depth_class: the largest
-// per-axis distance outside, quantised down).  The clamped cell
+// lower bound on their depth outside the grid's box (depth_class: the
+// Euclidean distance to the box, quantised down).  The clamped cell
 // assignment (Solver.cu:35-37) puts every layer of the reference's boundary
 // shell that lies outside the grid into the edge cells, up to five layers on
 // each clamped axis.  A boundary particle j within h of a particle at x
@@ -162,9 +162,11 @@ struct DepthClass {
 __device__ __forceinline__ DepthClass depth_class(const GridParams& g, float x, float y, float z,
                                                   float quantum, int qb) {
     if (qb <= 0) return {0u, 0.0f};
-    float d = fmaxf(fmaxf(__fsub_rn(g.ox, x), __fsub_rn(x, g.ex)), 0.0f);
-    d = fmaxf(d, fmaxf(__fsub_rn(g.oy, y), __fsub_rn(y, g.ey)));
-    d = fmaxf(d, fmaxf(__fsub_rn(g.oz, z), __fsub_rn(z, g.ez)));
+    const float ax = fmaxf(fmaxf(__fsub_rn(g.ox, x), __fsub_rn(x, g.ex)), 0.0f);
+    const float ay = fmaxf(fmaxf(__fsub_rn(g.oy, y), __fsub_rn(y, g.ey)), 0.0f);
+    const float az = fmaxf(fmaxf(__fsub_rn(g.oz, z), __fsub_rn(z, g.ez)), 0.0f);
+    const float d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)),
+                                         __fmul_rn(az, az)));  // distance to the box
     float c = floorf(__fdiv_rn(d, quantum)) - 1.0f;
     c = fminf(fmaxf(c, 0.0f), (float)((1u << qb) - 1u));
     return {(uint32_t)c, __fmul_rn(c, quantum)};
