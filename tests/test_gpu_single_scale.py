@@ -1,6 +1,6 @@
 """Single-scale parity: the CUDA path (through the C ABI) against the FP64 oracle.
 
-Bars (BASELINE the benchmark spec):
+Bars:
   * cell keys, sorted order, cell ranges, neighbour counts: bit-exact;
   * per-step density: |rho - rho_oracle| / rho_oracle <= 1e-5 per particle;
   * per-step acceleration: max_i |a_i - a_oracle,i| / max_i |a_oracle,i| <= 1e-5;
