@@ -144,6 +144,32 @@ def test_edge_cases_empty_single_clamped_coincident():
         check_step_against_oracle(s, cfg, b)
 
 
+def test_boundary_depth_cut_with_particles_outside_the_box():
+    """The boundary scan of a cell stops at the first boundary particle deeper
+    outside the grid's box than the fluid particle can reach.  A five-layer
+    shell around the box (the layers outside the grid pile up in the edge
+    cells) and fluid particles outside the box, up to 2.5 h deep, beside
+    faces, edges and corners: boundary neighbour counts bit-exact and
+    accelerations as the full scan gives them (the oracle)."""
+    h = 1.0 / 16
+    g = Grid.make_grid((0, 0, 0), (1, 1, 1), h)
+    cfg = SolverConfiguration.direct(h, (h / 2) ** 3 * 1000, 1000.0, 30.0, 5.0, 88.1472, 0.8, g)
+    shell = ParticleData.create_particle_box_canvas(Grid.make_grid((0, 0, 0), (1, 1, 1), h / 2), 5)
+    rng = np.random.default_rng(5)
+    inside = rng.uniform(0.0, 1.0, (1500, 3))
+    depth = rng.uniform(0.0, 2.5 * h, (900, 1))
+    outside = rng.uniform(0.0, 1.0, (900, 3))
+    for k in range(900):  # push 1, 2 or 3 coordinates out through a face, edge or corner
+        axes = rng.choice(3, size=1 + k % 3, replace=False)
+        for a in axes:
+            outside[k, a] = -depth[k, 0] if rng.random() < 0.5 else 1.0 + depth[k, 0]
+    x = np.concatenate([inside, outside]).astype(np.float32)
+    with Solver(ParticleData(x), shell, cfg) as s:
+        check_step_against_oracle(s, cfg, shell.positions)
+        d = s.debug_step_fields()
+        assert d["nbr_boundary"].max() > 20  # particles deep in the shell
+
+
 def test_non_cubic_grid_and_non_power_of_two_dims():
     g = Grid.make_grid((-0.1, -0.1, -0.2), (1.7, 1.6, 0.6), 0.0203)
     cfg = SolverConfiguration.direct(0.0203, 0.0075 ** 3 * 1000, 1000.0, 30.0, 5.0, 88.1472, 0.8, g)
