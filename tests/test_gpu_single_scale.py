@@ -170,6 +170,21 @@ def test_boundary_depth_cut_with_particles_outside_the_box():
         assert d["nbr_boundary"].max() > 20  # particles deep in the shell
 
 
+def test_boundary_scan_without_depth_cut_far_from_the_origin():
+    """A grid at x ~ 1000 with h = 1/16: the depth classes (h/16) would sit
+    near the coordinates' rounding, so the presort leaves them out and every
+    boundary cell is scanned in full; parity as everywhere else."""
+    h = 1.0 / 16
+    o = (1000.0, 1000.0, 1000.0)
+    g = Grid.make_grid(o, (1001.0, 1001.0, 1001.0), h)
+    cfg = SolverConfiguration.direct(h, (h / 2) ** 3 * 1000, 1000.0, 30.0, 5.0, 88.1472, 0.8, g)
+    shell = ParticleData.create_particle_box_canvas(Grid.make_grid(o, (1001.0, 1001.0, 1001.0), h / 2), 3)
+    rng = np.random.default_rng(6)
+    x = (np.float32(1000.0) + rng.uniform(-0.1, 1.1, (1500, 3))).astype(np.float32)
+    with Solver(ParticleData(x), shell, cfg) as s:
+        check_step_against_oracle(s, cfg, shell.positions)
+
+
 def test_non_cubic_grid_and_non_power_of_two_dims():
     g = Grid.make_grid((-0.1, -0.1, -0.2), (1.7, 1.6, 0.6), 0.0203)
     cfg = SolverConfiguration.direct(0.0203, 0.0075 ** 3 * 1000, 1000.0, 30.0, 5.0, 88.1472, 0.8, g)
