@@ -94,7 +94,7 @@ int enqueue_neighborhood(sph_batch* b) {
     cudaMemsetAsync(b->cells, 0xFF, sizeof(uint2) * b->NC, st);
     sort_reset(b->sort, st);
     b_hash_hist_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
-        b->tiles[1], b->ntiles[1], b->recs, b->pos, b->shift, b->passes, false, b->keys[0],
+        b->tiles[1], b->ntiles[1], b->recs, b->pos, b->shift, b->passes, b->keys[0],
         b->sort.hist);
     sort_scan(b->passes, b->sort, st);
     const int o = sort_passes_run(b->keys, b->vals, nullptr, b->N, b->passes, b->sort, b->err, 0, st);

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(BS) b_hash_hist_kernel(const uint2* __restrict
                                                          uint32_t num_tiles,
                                                          const SceneRec* __restrict__ recs,
                                                          const float4* __restrict__ pos,
-                                                         int shift, int passes, bool boundary,
+                                                         int shift, int passes,
                                                          uint32_t* __restrict__ keys,
                                                          uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[kSortMaxPasses][256];
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(BS) b_hash_hist_kernel(const uint2* __restrict
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
         const SceneRec& R = recs[tile.x];
-        const uint32_t end = boundary ? R.b_off + R.b_n : R.p_off + R.p_n;
+        const uint32_t end = R.p_off + R.p_n;
         const uint32_t i = tile.y + threadIdx.x;
         if (i < end) {
             const float4 p = pos[i];
