@@ -1,9 +1,10 @@
-"""The C ABI from compiled code: tests/cabi_client.cpp is the reference-side
-adapter (the `Solver` class that forwards to include/sph2s.h) driving a scene
-built with the ABI's grid, particle-box and configuration builders.
+"""The C ABI from compiled code: tests/cabi_client.cpp and tests/cabi_client2.cpp
+are the reference-side adapters (the single-scale and two-scale `Solver`
+classes that forward to include/sph2s.h), each driving a scene built with the
+ABI's grid, particle-box and configuration builders.
 
-CPU: the header compiles as C99 and as C++17 with warnings as errors, and the
-client links against libsph2s.so.  GPU: the client's run equals the same run
+CPU: the header compiles as C99 and as C++17 with warnings as errors, and both
+clients link against libsph2s.so.  GPU: each client's run equals the same run
 through the Python binding bit for bit (same library, same inputs)."""
 import ctypes as C
 import shutil
@@ -16,6 +17,7 @@ import pytest
 
 from sph2s_final_gb300 import _abi
 from sph2s_final_gb300.solver import ParticleData, Solver
+from sph2s_final_gb300.two_scale import HIGH, LOW, STAT_NAMES, Solver2
 
 ROOT = Path(__file__).resolve().parents[1]
 PKG = ROOT / "sph2s_final_gb300"
@@ -28,11 +30,11 @@ def compiler(name):
     return exe
 
 
-def build_client(tmp_path):
+def build_client(tmp_path, name="cabi_client"):
     _abi.lib()  # the library is built (raises with the build command otherwise)
-    exe = tmp_path / "cabi_client"
+    exe = tmp_path / name
     cmd = [compiler("g++"), "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
-           "-I", str(ROOT / "include"), str(ROOT / "tests" / "cabi_client.cpp"),
+           "-I", str(ROOT / "include"), str(ROOT / "tests" / f"{name}.cpp"),
            "-L", str(PKG), "-lsph2s", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -48,8 +50,9 @@ def test_header_compiles_as_c(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-def test_client_compiles_and_links(tmp_path):
-    assert build_client(tmp_path).exists()
+@pytest.mark.parametrize("name", ["cabi_client", "cabi_client2"])
+def test_client_compiles_and_links(tmp_path, name):
+    assert build_client(tmp_path, name).exists()
 
 
 def read_run(path):
@@ -87,3 +90,50 @@ def test_client_run_equals_python_binding(tmp_path):
         np.testing.assert_array_equal(s.positions("by_id"), x)
         np.testing.assert_array_equal(s.densities("by_id"), rho)
     assert np.abs(x - fluid).max() > 0  # the client did step the scene
+
+
+def read_run2(path):
+    data = path.read_bytes()
+    nl, nb, steps = struct.unpack_from("<III", data, 0)
+    (dt,) = struct.unpack_from("<f", data, 12)
+    off = 16
+    cfg = _abi.sph_config2.from_buffer_copy(data, off)
+    off += C.sizeof(_abi.sph_config2)
+
+    def take(dtype, count):
+        nonlocal off
+        a = np.frombuffer(data, dtype, count, off).copy()
+        off += 4 * count
+        return a
+
+    low = take(np.float32, 3 * nl).reshape(nl, 3)
+    boundary = take(np.float32, 3 * nb).reshape(nb, 3)
+    stats = dict(zip(STAT_NAMES, map(int, take(np.uint32, 6))))
+    pops = []
+    for _ in (LOW, HIGH):
+        (n,) = struct.unpack_from("<I", data, off)
+        off += 4
+        pops.append({"ids": take(np.uint32, n), "x": take(np.float32, 3 * n).reshape(n, 3),
+                     "v": take(np.float32, 3 * n).reshape(n, 3), "lam": take(np.float32, n),
+                     "state": take(np.int32, n), "group": take(np.uint32, n)})
+    assert off == len(data)
+    return cfg, low, boundary, steps, dt, stats, pops
+
+
+@pytest.mark.gpu
+def test_two_scale_client_run_equals_python_binding(tmp_path):
+    exe = build_client(tmp_path, "cabi_client2")
+    out = tmp_path / "run2.bin"
+    r = subprocess.run([str(exe), str(out), "30"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cfg, low, boundary, steps, dt, stats, pops = read_run2(out)
+    assert low.shape == (4096, 3) and steps == 30 and cfg.refine_axis == 0
+    assert pops[HIGH]["ids"].size > 0  # the slab refined part of the block
+    with Solver2(low, None, boundary, cfg) as s:
+        s.advance(dt, steps)
+        assert s.last_stats() == stats
+        for pop in (LOW, HIGH):
+            st = s.state(pop)
+            for k in ("ids", "x", "v", "lam", "state", "group"):
+                np.testing.assert_array_equal(st[k], pops[pop][k], err_msg=f"{pop} {k}")
+    assert np.isfinite(pops[LOW]["x"]).all() and np.isfinite(pops[HIGH]["x"]).all()
