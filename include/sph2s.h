@@ -186,6 +186,14 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms);
  * bounded spin, so the next sph_sync returns SPH_E_TIMEOUT without hanging. */
 int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on);
 
+/* Test hook selecting how each step sorts its (cell key, index) pairs; both
+ * ways give the same permutation.  0 (default): automatic -- coherent from
+ * 131,072 particles on, from scratch below (where the radix sort alone is
+ * faster); 1: from scratch (sph_sort_pairs' onesweep sort); 2: coherent
+ * (sph_sort_keys_coherent's scheme: only the particles that changed cell
+ * since the last step are radix-sorted, the rest merged around them). */
+int sph_debug_sort_mode(sph_solver* s, int32_t mode);
+
 /* ---- differentiable rollout (no counterpart in the reference) ------------ */
 
 /* Restarts the solver from its creation positions with initial velocities
@@ -400,6 +408,20 @@ int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* k
  * and must be serialised by the caller. */
 int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                            uint32_t* vals_out, uint32_t n, int32_t key_bits, void* stream);
+
+/* The step's coherent sort on keys in device memory (no counterpart in the
+ * reference): the stable ascending order of n keys (low `key_bits` bits, the
+ * others 0), given `hint`, any non-decreasing array of n uint32 in device
+ * memory -- typically the same objects' sorted keys of a moment earlier.
+ * keys_out = the sorted keys and perm_out[i] = the input index of the i-th
+ * of them, exactly sph_sort_pairs with values 0..n-1, for every hint; the
+ * hint sets only the cost: keys that differ from the hint at their own index
+ * are radix-sorted, the others merged around them in one pass.  A hint that
+ * decreases anywhere: SPH_E_INVALID, outputs untouched.  Enqueues on
+ * `stream`, allocates its scratch with cudaMalloc, and returns after the sort
+ * completed. */
+int sph_sort_keys_coherent(const uint32_t* keys_in, const uint32_t* hint, uint32_t* keys_out,
+                           uint32_t* perm_out, uint32_t n, int32_t key_bits, void* stream);
 
 /* Description of the last failure on the calling thread ("" if none). */
 const char* sph_last_error(void);

@@ -111,6 +111,7 @@ SIGNATURES = {
     "sph_debug_step_fields": (C.c_int, [_vp, _u, _u, _u, _u, _u, _u, _f, _f]),
     "sph_profile_phases": (C.c_int, [_vp, C.c_float, C.c_int32, _f]),
     "sph_debug_force_lookback_timeout": (C.c_int, [_vp, C.c_int32]),
+    "sph_debug_sort_mode": (C.c_int, [_vp, C.c_int32]),
     "sph_rollout_forward": (C.c_int, [_vp, _f, C.c_float, C.c_float, C.c_int32, C.c_int32]),
     "sph_rollout_density_loss": (C.c_int, [_vp, C.POINTER(sph_grid), _f, _f,
                                            C.POINTER(C.c_double)]),
@@ -144,6 +145,8 @@ SIGNATURES = {
     "sph_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                  C.c_int32, C.c_void_p]),
     "sph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_uint32, C.c_int32, C.c_void_p]),
+    "sph_sort_keys_coherent": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_uint32, C.c_int32, C.c_void_p]),
     "sph_set_integrator": (C.c_int, [_vp, C.c_int32]),
     "sph_step_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),

@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(256) scan_kernel(uint32_t* hist, int passes) {
 
 __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+    const uint32_t* __restrict__ n_dev, uint32_t small_max, int shift,
     const uint32_t* __restrict__ digit_offsets, uint32_t* status, uint32_t* tile_ctr,
     uint32_t* err, int force_timeout) {
     __shared__ uint32_t s_keys[kSortTile];
@@ -82,18 +83,26 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     __shared__ uint32_t s_tile;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int ni = kSortItems;  // keys per thread
+    if (n_dev) {  // key count known on the device only: the grid covers n keys
+        n = min(*n_dev, n);
+        if (n == 0) return;
+        if (n <= small_max) ni = kSortItemsSmall;  // few keys: more, smaller tiles
+    }
+    const uint32_t tile_keys = (uint32_t)ni * kSortThreads;
     if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
     for (int i = tid; i < kWarps * 257; i += kSortThreads) (&s_whist[0][0])[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
-    const uint32_t base = tile * (uint32_t)kSortTile;
-    const uint32_t seg = base + (uint32_t)warp * (kSortItems * 32);
+    const uint32_t base = tile * tile_keys;
+    if (base >= n) return;  // tiles are handed out in order: no later tile waits on this one
+    const uint32_t seg = base + (uint32_t)warp * ((uint32_t)ni * 32);
 
     uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = seg + i * 32 + lane;
-        bool ok = idx < n;
+        bool ok = i < ni && idx < n;
         k[i] = ok ? keys_in[idx] : 0xFFFFFFFFu;
         v[i] = ok ? (vals_in ? vals_in[idx] : idx) : 0u;
     }
@@ -101,6 +110,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
+        if (i >= ni) break;
         uint32_t idx = seg + i * 32 + lane;
         uint32_t d = idx < n ? ((k[i] >> shift) & 255u) : 256u;
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
@@ -155,7 +165,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
         uint32_t idx = seg + i * 32 + lane;
-        if (idx < n) {
+        if (i < ni && idx < n) {
             uint32_t d = (k[i] >> shift) & 255u;
             uint32_t pos = s_local_start[d] + s_whist[warp][d] + rank[i];
             s_keys[pos] = k[i];
@@ -164,7 +174,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     }
     __syncthreads();
 
-    const uint32_t tile_n = (n - base) < (uint32_t)kSortTile ? (n - base) : (uint32_t)kSortTile;
+    const uint32_t tile_n = (n - base) < tile_keys ? (n - base) : tile_keys;
     for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
         uint32_t key = s_keys[i];
         uint32_t g = s_gbase[(key >> shift) & 255u] + i;
@@ -223,24 +233,36 @@ void sort_pass(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
     if (n == 0) return;
     uint32_t tiles = (n + kSortTile - 1) / kSortTile;
     onesweep_kernel<<<tiles, kSortThreads, 0, st>>>(
-        keys_in, vals_in, keys_out, vals_out, n, 8 * p, s.hist + p * 256,
+        keys_in, vals_in, keys_out, vals_out, n, nullptr, 0u, 8 * p, s.hist + p * 256,
         s.status + (size_t)p * s.max_tiles * 256, s.tile_ctr + p, err, force_timeout);
+}
+
+int sort_passes_run_dev(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals,
+                        uint32_t n, const uint32_t* n_dev, uint32_t small_max, int passes,
+                        const SortScratch& s, uint32_t* err, int force_timeout, cudaStream_t st) {
+    if (n == 0) return 0;
+    uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+    if (n_dev) {
+        const uint32_t few = n < small_max ? n : small_max;
+        const uint32_t small_tiles = (few + kSortTileSmall - 1) / kSortTileSmall;
+        if (small_tiles > tiles) tiles = small_tiles;
+    }
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t* vin = (p == 0) ? first_vals : vals[cur];
+        onesweep_kernel<<<tiles, kSortThreads, 0, st>>>(
+            keys[cur], vin, keys[cur ^ 1], vals[cur ^ 1], n, n_dev, small_max, 8 * p, s.hist + p * 256,
+            s.status + (size_t)p * s.max_tiles * 256, s.tile_ctr + p, err, force_timeout);
+        cur ^= 1;
+    }
+    return cur;
 }
 
 int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals, uint32_t n,
                     int passes, const SortScratch& s, uint32_t* err, int force_timeout,
                     cudaStream_t st) {
-    if (n == 0) return 0;
-    uint32_t tiles = (n + kSortTile - 1) / kSortTile;
-    int cur = 0;
-    for (int p = 0; p < passes; ++p) {
-        const uint32_t* vin = (p == 0) ? first_vals : vals[cur];
-        onesweep_kernel<<<tiles, kSortThreads, 0, st>>>(
-            keys[cur], vin, keys[cur ^ 1], vals[cur ^ 1], n, 8 * p, s.hist + p * 256,
-            s.status + (size_t)p * s.max_tiles * 256, s.tile_ctr + p, err, force_timeout);
-        cur ^= 1;
-    }
-    return cur;
+    return sort_passes_run_dev(keys, vals, first_vals, n, nullptr, 0u, passes, s, err,
+                               force_timeout, st);
 }
 
 int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int key_bits,

@@ -22,6 +22,10 @@ namespace sph {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys
+// Device-counted sorts of at most small_max keys use tiles of 512 keys: twice
+// the tiles run in parallel per 1,024 keys and each tile's chain is 8x shorter.
+constexpr int kSortItemsSmall = 2;
+constexpr int kSortTileSmall = kSortThreads * kSortItemsSmall;
 constexpr int kSortMaxPasses = 4;
 
 // Device scratch of one sort plan.  Everything that must start at zero lives
@@ -66,6 +70,16 @@ void sort_scan(int passes, const SortScratch& s, cudaStream_t st);
 int sort_passes_run(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals, uint32_t n,
                     int passes, const SortScratch& s, uint32_t* err, int force_timeout,
                     cudaStream_t st);
+
+// sort_passes_run for a key count that only the device knows: each pass sorts
+// m = min(*n_dev, n) keys, in tiles of kSortTileSmall keys when m <= small_max
+// and of kSortTile keys otherwise; the grid covers both cases and tiles
+// beyond m exit at once.  The plan's status area must hold
+// max(tiles of n, small tiles of min(n, small_max)) tiles per pass
+// (sort_scratch_bytes(max(n, 8 * min(n, small_max)))).
+int sort_passes_run_dev(uint32_t* keys[2], uint32_t* vals[2], const uint32_t* first_vals,
+                        uint32_t n, const uint32_t* n_dev, uint32_t small_max, int passes,
+                        const SortScratch& s, uint32_t* err, int force_timeout, cudaStream_t st);
 
 // One digit pass p (bits 8p..8p+7) from explicit input to output buffers
 // (vals_in NULL: values are the input indices).  Needs the histograms of

@@ -26,7 +26,7 @@ int free_solver(sph_solver* s) {
     if (s->graph) cudaGraphExecDestroy(s->graph);
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
-                    s->bpos,    s->sort_mem, s->err,     s->stage, s->nbr, s->nbr_count,
+                    s->bpos,    s->sort_mem, s->co_mem,  s->err,   s->stage, s->nbr, s->nbr_count,
                     s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -53,20 +53,32 @@ int dalloc(T** p, size_t count) {
 
 namespace sph_ss {
 
-// hash -> onesweep sort -> reorder + cell ranges (Solver.cu:1098-1140).
+// hash -> stable sort of (cell key, index) -> reorder + cell ranges
+// (Solver.cu:1098-1140).  The sort is the coherent one (coherent_sort.cuh):
+// the same permutation as sorting from scratch, at the cost of the particles
+// that changed cell since the last step.
 int enqueue_neighborhood(sph_solver* s) {
     cudaStream_t st = s->stream;
-    int passes = sort_passes(s->key_bits);
+    int out = 1;
+    const bool coherent = s->sort_mode == kSortCoherent ||
+                          (s->sort_mode == kSortAuto && s->n >= kCoherentMinParticles);
+    if (!coherent || s->force_timeout) {
+        const int passes = sort_passes(s->key_bits);
+        sort_reset(s->sort, st);
+        uint32_t hb = blocks_for(s->n);
+        if (hb > 152 * 8) hb = 152 * 8;
+        hash_hist_kernel<<<hb, 256, 0, st>>>(s->pos, s->n, s->P.g, passes, s->keys[0], s->sort.hist);
+        sort_scan(passes, s->sort, st);
+        out = sort_passes_run(s->keys, s->vals, nullptr, s->n, passes, s->sort, s->err, s->force_timeout, st);
+    } else {  // sort, reorder and cell table in one sequence
+        coherent_sort_cells(s->co, s->pos, s->vel, s->P.g, s->cells, s->key_bits, s->keys[0],
+                            s->keys[1], s->vals[1], s->spos, s->svel, s->err, s->force_timeout, st);
+        return out;
+    }
     cudaMemsetAsync(s->cells, 0xFF, sizeof(uint2) * s->ncells, st);
-    sort_reset(s->sort, st);
-    uint32_t hb = blocks_for(s->n);
-    if (hb > 152 * 8) hb = 152 * 8;
-    hash_hist_kernel<<<hb, 256, 0, st>>>(s->pos, s->n, s->P.g, passes, s->keys[0], s->sort.hist);
-    sort_scan(passes, s->sort, st);
-    int out = sort_passes_run(s->keys, s->vals, nullptr, s->n, passes, s->sort, s->err, s->force_timeout, st);
     gather_cells_kernel<true><<<blocks_for(s->n), 256, 0, st>>>(
         s->keys[out], s->vals[out], s->n, s->P.g, s->pos, s->vel, s->spos, s->svel, s->cells,
-        s->err);
+        s->err, 0, s->co.kprev);
     return out;
 }
 
@@ -128,6 +140,7 @@ int check_device_error(sph_solver* s) {
     uint32_t e = *s->err_host;
     if (e) {
         SPH_CUDA(cudaMemsetAsync(s->err, 0, 4, s->stream));
+        coherent_reset(s->co, s->stream);  // the stored sorted keys may be garbage now
         SPH_CUDA(cudaStreamSynchronize(s->stream));
         if (e & kErrLookbackTimeout)
             return fail(SPH_E_TIMEOUT, "radix sort look-back timed out; step results are invalid");
@@ -177,12 +190,16 @@ int create_solver(const sph_config* config, const float4* hpos, const float4* hv
     TRY(dalloc(&s->keys[1], nmax));
     TRY(dalloc(&s->vals[0], nmax));
     TRY(dalloc(&s->vals[1], nmax));
-    TRY(dalloc(&s->cells, s->ncells));
     TRY(dalloc(&s->bcells, s->ncells));
     TRY(dalloc(&s->bpos, n_boundary));
     TRY(dalloc(&s->pos0, n_fluid));
     TRY(check_cuda(cudaMalloc(&s->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
     s->sort = sort_scratch_from(s->sort_mem, nmax);
+    TRY(dalloc(&s->cells, s->ncells));  // read by the first coherent sort: no stale ranges
+    TRY(check_cuda(cudaMemsetAsync(s->cells, 0xFF, sizeof(uint2) * s->ncells, s->stream), "memset", __FILE__, __LINE__));
+    TRY(check_cuda(cudaMalloc(&s->co_mem, coherent_bytes(n_fluid)), "sort scratch", __FILE__, __LINE__));
+    s->co = coherent_from(s->co_mem, n_fluid);
+    coherent_reset(s->co, s->stream);
     TRY(dalloc(&s->err, 1));
     TRY(check_cuda(cudaMallocHost((void**)&s->err_host, 4), "pinned", __FILE__, __LINE__));
     TRY(check_cuda(cudaMemsetAsync(s->err, 0, 4, s->stream), "memset", __FILE__, __LINE__));
@@ -447,7 +464,7 @@ int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t
     SPH_CUDA(cudaMalloc(&dacc, 12 * (size_t)n));
     SPH_CUDA(cudaMalloc(&dnf, 4 * (size_t)n));
     SPH_CUDA(cudaMalloc(&dnb, 4 * (size_t)n));
-    enqueue_neighborhood(s);
+    const int out = enqueue_neighborhood(s);  // buffer index holding the sorted keys
     density_kernel<true><<<blocks_for(n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
         s->spos, s->cells, n, s->P, drho, daux, s->nbr, s->nbr_count, dnf, s->xa, s->svel);
     force_kernel<1><<<blocks_for(n), 256, 0, s->stream>>>(
@@ -455,7 +472,6 @@ int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t
         s->nb, s->P, 0.0f, nullptr, nullptr, dacc, dnb);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    int out = sort_passes(s->key_bits) & 1;  // buffer index holding the sorted keys
     std::vector<float4> sp;
     if (e == cudaSuccess && keys) e = cudaMemcpy(keys, s->keys[out], 4 * (size_t)n, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && ids) {
@@ -517,6 +533,19 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms) {
 int sph_debug_force_lookback_timeout(sph_solver* s, int32_t on) {
     if (!s) return fail(SPH_E_INVALID, "NULL handle");
     s->force_timeout = on ? 1 : 0;
+    return SPH_OK;
+}
+
+int sph_debug_sort_mode(sph_solver* s, int32_t mode) {
+    if (!s) return fail(SPH_E_INVALID, "NULL handle");
+    if (mode != kSortAuto && mode != kSortFull && mode != kSortCoherent)
+        return fail(SPH_E_INVALID, "sph_debug_sort_mode: mode must be 0, 1 or 2");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    s->sort_mode = mode;
     return SPH_OK;
 }
 

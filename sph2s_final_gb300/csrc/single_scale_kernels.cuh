@@ -63,7 +63,8 @@ static __global__ void __launch_bounds__(256) boundary_hash_hist_kernel(
 }
 
 // Reorders the state by the sorted permutation and records cell ranges (keys
-// shifted right by key_shift first: the boundary presort's depth bits).
+// shifted right by key_shift first: the boundary presort's depth bits); with
+// kprev_out, also stores the sorted keys for the next coherent sort.
 // Every index read from the sort output is range-checked: if a bounded wait in
 // the sort gave up, its output is garbage, and this kernel then records an
 // error and stays in bounds instead of faulting.
@@ -72,9 +73,10 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     GridParams g, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err, int key_shift = 0) {
+    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (kprev_out) kprev_out[i] = keys_sorted[i];  // the next step's coherent sort starts here
     uint32_t q = perm[i];
     if (q >= n) {
         atomicOr(err, 2u);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include "../../include/sph2s.h"
 #include "common.cuh"
+#include "coherent_sort.cuh"
 #include "radix_sort.cuh"
 
 namespace sph {
@@ -35,6 +36,9 @@ struct sph_solver {
     float* stage = nullptr;  // device staging for packed readback
     void* sort_mem = nullptr;
     sph::SortScratch sort;
+    void* co_mem = nullptr;   // scratch of the coherent sort
+    sph::CoherentSort co;
+    int sort_mode = 0;        // kSortAuto / kSortFull / kSortCoherent (sph_debug_sort_mode)
     uint32_t* err = nullptr;  // device error word
     uint32_t* err_host = nullptr;
     int force_timeout = 0;
@@ -54,8 +58,13 @@ struct sph_solver {
 };
 
 namespace sph_ss {
-// hash -> onesweep sort -> reorder + cell ranges; returns the index of the
-// key/value buffers that hold the sorted keys and the permutation.
+// The step's sort: automatic (coherent from kCoherentMinParticles on, where it
+// is faster on GB300), from scratch, or coherent.
+constexpr int kSortAuto = 0, kSortFull = 1, kSortCoherent = 2;
+constexpr uint32_t kCoherentMinParticles = 131072;
+// hash -> sort (coherent or from scratch, sort_mode) -> reorder + cell ranges;
+// returns the index of the key/value buffers that hold the sorted keys and
+// the permutation.
 int enqueue_neighborhood(sph_solver* s);
 void enqueue_density(sph_solver* s);
 void enqueue_force(sph_solver* s, float dt);

@@ -5,6 +5,7 @@
 // boundary): ascending by key, stable (equal keys keep their input order).
 #include <cstring>
 #include "errors.h"
+#include "coherent_sort.cuh"
 #include "radix_sort.cuh"
 
 using namespace sph;
@@ -56,5 +57,54 @@ extern "C" int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     cudaFree(err);
     SPH_CUDA(e);
     if (herr) return fail(SPH_E_TIMEOUT, "sph_sort_pairs: look-back timed out; output invalid");
+    return SPH_OK;
+}
+
+namespace {
+
+__global__ void nondecreasing_check_kernel(const uint32_t* __restrict__ a, uint32_t n,
+                                           uint32_t* __restrict__ bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 < n && a[i] > a[i + 1]) *bad = 1u;
+}
+
+}  // namespace
+
+extern "C" int sph_sort_keys_coherent(const uint32_t* keys_in, const uint32_t* hint,
+                                      uint32_t* keys_out, uint32_t* perm_out, uint32_t n,
+                                      int32_t key_bits, void* stream) {
+    if (n == 0) return SPH_OK;
+    if (!keys_in || !hint || !keys_out || !perm_out)
+        return fail(SPH_E_INVALID, "sph_sort_keys_coherent: NULL pointer");
+    if (key_bits < 1 || key_bits > 32)
+        return fail(SPH_E_INVALID, "sph_sort_keys_coherent: key_bits must be in 1..32");
+    if (n > (1u << 30)) return fail(SPH_E_CAPACITY, "sph_sort_keys_coherent: more than 2^30 keys");
+    cudaStream_t st = (cudaStream_t)stream;
+    void* co_mem = nullptr;
+    uint32_t* err = nullptr;  // [0] sort errors, [1] hint out of order
+    cudaError_t e = cudaMalloc(&co_mem, coherent_bytes(n));
+    if (e == cudaSuccess) e = cudaMalloc(&err, 8);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, 8, st);
+    uint32_t herr[2] = {0, 0};
+    if (e == cudaSuccess) {
+        nondecreasing_check_kernel<<<(n + 255) / 256, 256, 0, st>>>(hint, n, err + 1);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    if (e == cudaSuccess && !herr[1]) {
+        CoherentSort c = coherent_from(co_mem, n);
+        c.kprev = const_cast<uint32_t*>(hint);  // read only: the step's gather writes it
+        coherent_sort_keys(c, keys_in, key_bits, keys_out, perm_out, err, 0, st);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    cudaFree(co_mem);
+    cudaFree(err);
+    SPH_CUDA(e);
+    if (herr[1]) return fail(SPH_E_INVALID, "sph_sort_keys_coherent: hint is not non-decreasing");
+    if (herr[0] & 1u) return fail(SPH_E_TIMEOUT, "sph_sort_keys_coherent: look-back timed out; output invalid");
+    if (herr[0]) return fail(SPH_E_CAPACITY, "sph_sort_keys_coherent: placement out of range");
     return SPH_OK;
 }

@@ -235,6 +235,13 @@ class Solver:
     def debug_force_lookback_timeout(self, on: bool) -> None:
         check(lib().sph_debug_force_lookback_timeout(self._h, 1 if on else 0))
 
+    SORT_MODES = {"auto": 0, "full": 1, "coherent": 2}
+
+    def debug_sort_mode(self, mode: str) -> None:
+        """Test hook: how each step sorts ("auto", "full" = from scratch,
+        "coherent" = only the particles that changed cell); same results."""
+        check(lib().sph_debug_sort_mode(self._h, self.SORT_MODES[mode]))
+
     def positions_async(self, out: np.ndarray, order: str = "sorted") -> None:
         """Enqueues a readback of the positions into `out` (float32 (n, 3), best
         pinned); valid after sync().  The copy overlaps the next steps."""
