@@ -89,18 +89,29 @@ void enqueue_force(sph_batch* b, float dt) {
     }
 }
 
+// hash -> stable sort of (scene, cell key, index) -> reorder + cell ranges.
+// From 131,072 fluid particles the sort is the coherent one (coherent_sort.cuh:
+// the same permutation, radix-sorting only the particles that changed cell).
 int enqueue_neighborhood(sph_batch* b) {
     cudaStream_t st = b->stream;
     cudaMemsetAsync(b->cells, 0xFF, sizeof(uint2) * b->NC, st);
-    sort_reset(b->sort, st);
-    b_hash_hist_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
-        b->tiles[1], b->ntiles[1], b->recs, b->pos, b->shift, b->passes, b->keys[0],
-        b->sort.hist);
-    sort_scan(b->passes, b->sort, st);
-    const int o = sort_passes_run(b->keys, b->vals, nullptr, b->N, b->passes, b->sort, b->err, 0, st);
+    int o = 1;
+    if (b->coherent) {
+        b_hash_hist_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
+            b->tiles[1], b->ntiles[1], b->recs, b->pos, b->shift, 0, b->keys[0], b->sort.hist);
+        coherent_sort_keys(b->co, b->keys[0], 8 * b->passes, b->keys[1], b->vals[1], b->err, 0,
+                           st);
+    } else {
+        sort_reset(b->sort, st);
+        b_hash_hist_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
+            b->tiles[1], b->ntiles[1], b->recs, b->pos, b->shift, b->passes, b->keys[0],
+            b->sort.hist);
+        sort_scan(b->passes, b->sort, st);
+        o = sort_passes_run(b->keys, b->vals, nullptr, b->N, b->passes, b->sort, b->err, 0, st);
+    }
     b_gather_cells_kernel<256, true><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
         b->tiles[1], b->ntiles[1], b->recs, b->keys[o], b->vals[o], b->N, b->shift, false, b->pos,
-        b->vel, b->spos, b->svel, b->cells, b->err);
+        b->vel, b->spos, b->svel, b->cells, b->err, 0, b->coherent ? b->co.kprev : nullptr);
     return o;
 }
 
@@ -128,6 +139,7 @@ int check_err(sph_batch* b) {
     const uint32_t e = *b->err_host;
     if (e) {
         SPH_CUDA(cudaMemsetAsync(b->err, 0, 4, b->stream));
+        if (b->coherent) coherent_reset(b->co, b->stream);  // the kept keys may be garbage
         SPH_CUDA(cudaStreamSynchronize(b->stream));
         if (e & kErrLookbackTimeout) return fail(SPH_E_TIMEOUT, "radix sort look-back timed out");
         return fail(SPH_E_CAPACITY, "device-side index check failed");
@@ -222,6 +234,13 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(check_cuda(cudaMalloc(&b->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
     b->owned.push_back(b->sort_mem);
     b->sort = sort_scratch_from(b->sort_mem, nmax);
+    b->coherent = b->N >= 131072u;
+    if (b->coherent) {
+        TRY(check_cuda(cudaMalloc(&b->co_mem, coherent_bytes(b->N)), "sort scratch", __FILE__, __LINE__));
+        b->owned.push_back(b->co_mem);
+        b->co = coherent_from(b->co_mem, b->N);
+        TRY(check_cuda(cudaMemset(b->co.kprev, 0xFF, 4 * (size_t)b->N), "memset", __FILE__, __LINE__));
+    }
     TRY(dalloc(&b->err, 1, b->owned));
     TRY(check_cuda(cudaMemset(b->err, 0, 4), "memset", __FILE__, __LINE__));
     TRY(check_cuda(cudaMallocHost((void**)&b->err_host, 4), "pinned", __FILE__, __LINE__));

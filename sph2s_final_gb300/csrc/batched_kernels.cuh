@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     int shift, bool boundary, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err, int key_shift = 0) {
+    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr) {
     const uint32_t lmask = (1u << shift) - 1u;
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
         const uint32_t end = beg + (boundary ? R.b_n : R.p_n);
         const uint32_t i = tile.y + threadIdx.x;
         if (i >= end) continue;
+        if (kprev_out) kprev_out[i] = keys_sorted[i];  // the next coherent sort starts here
         uint32_t q = perm[i];
         if (q < beg || q >= end) {  // a sort that gave up: stay in bounds, report
             atomicOr(err, 2u);

@@ -5,6 +5,7 @@
 #include <vector>
 #include "../../include/sph2s.h"
 #include "batched_kernels.cuh"
+#include "coherent_sort.cuh"
 #include "radix_sort.cuh"
 
 namespace sph {
@@ -35,6 +36,9 @@ struct sph_batch {
     float4* bpos = nullptr;
     void* sort_mem = nullptr;
     SortScratch sort;
+    void* co_mem = nullptr;  // the step's coherent sort (from 131,072 fluid particles on)
+    sph::CoherentSort co;
+    bool coherent = false;
     uint32_t* err = nullptr;
     uint32_t* err_host = nullptr;
     // tiles per block-size choice (fluid), boundary tiles at 256
