@@ -112,6 +112,10 @@ def test_null_handles_and_bad_arguments_return_status_codes():
     assert lib.sph_particle_box_canvas(C.byref(g), -1, None, 0, C.byref(n)) == _abi.SPH_E_INVALID
     with pytest.raises(_abi.SphError):
         Grid.make_grid((0, 0, 0), (1, 1, 1), -1.0)
+    # the coherent sort and the sort-mode hook check their arguments first
+    assert lib.sph_sort_keys_coherent(None, None, None, None, 0, 21, None) == _abi.SPH_OK
+    assert lib.sph_sort_keys_coherent(None, None, None, None, 9, 21, None) == _abi.SPH_E_INVALID
+    assert lib.sph_debug_sort_mode(None, 1) == _abi.SPH_E_INVALID
 
 
 def test_create_rejects_invalid_config_before_touching_the_device():
