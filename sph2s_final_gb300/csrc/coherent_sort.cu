@@ -177,7 +177,9 @@ __device__ __forceinline__ uint32_t movers_below_key(const uint32_t* __restrict_
 
 // Places every particle: blocks [0, kMoverBlocks) the sorted movers
 // (grid-stride; first, so that their searches of kprev overlap the rest), the
-// others one index per thread, which places it if it is a stayer.  Every
+// others one index per thread, which places it if it is a stayer.  Each writes
+// its key and input index at the destination and, with out_a / out_b, its two
+// float4 records (the step's positions and velocities in sorted order).  Every
 // destination is range-checked (a sort that gave up on a bounded wait leaves
 // garbage behind; the error word then already holds that failure).
 __global__ void __launch_bounds__(256) coherent_merge_kernel(
