@@ -100,8 +100,8 @@ def coherent_cases():
     rng = np.random.default_rng(7)
     out = []
     h = np.sort(rng.integers(0, 1 << 21, 300001).astype(np.uint32))
-    # one block sorts at most 12,288 changed keys; more go through the onesweep passes
-    for m in (0, 1, 5000, 12288, 12289, 100000, 300001):
+    # up to 32,768 changed keys are radix-sorted in tiles of 512, more in tiles of 4,096
+    for m in (0, 1, 5000, 32768, 32769, 100000, 300001):
         out.append((f"movers{m}", perturbed(h, m, 21, rng), h, 21))
     keys = rng.integers(0, 1 << 21, 50000).astype(np.uint32)
     out.append(("unrelated_hint", keys, np.sort(rng.integers(0, 1 << 21, 50000).astype(np.uint32)), 21))
