@@ -27,7 +27,7 @@ def lib():
     global _lib
     if _lib is None:
         if not LIB_PATH.exists():
-            from sph2s_final_gb300.build import build_oracle
+            from .build import build_oracle
             build_oracle()
         l = C.CDLL(str(LIB_PATH))
         l.or_thresh_sq.restype = C.c_float

@@ -1,21 +1,27 @@
-"""Builds the reference's own single-scale step kernels as a checker.
+"""Builds the reference's own step kernels as a checker, and drives them.
 
-Compiles SPH2S_FINAL_SINGLE_SCALE/Solver.cu, unmodified, from the reference
-checkout into oracle/_ref/ss_solver.cubin (sm_103a).  The reference is a
-Windows / CUDA 5.0 / OpenGL program; only its device code is wanted, and the
-translation unit needs a few header shims, written here into
-oracle/_ref/shims/:
+Compiles, unmodified, from a reference checkout named by the environment
+variable SPH2S_REFERENCE (the directory holding SPH2S_FINAL_SINGLE_SCALE/ etc.):
+  SPH2S_FINAL_SINGLE_SCALE/Solver.cu           -> oracle/_ref/ss_solver.cubin
+  SPH2S_FINAL_TWO_SCALE/Solver.cu              -> oracle/_ref/ts_solver.cubin
+  SPH2S_FINAL_TWO_SCALE_COUPLED/Solver.cu      -> oracle/_ref/cp_solver.cubin
+for sm_103a.  The reference is a Windows / CUDA 5.0 / OpenGL program; only its
+device code is wanted, and the translation units need a few header shims,
+written here into oracle/_ref/shims/:
   * Windows.h: empty;
   * cuda_gl_interop.h: GL handle typedefs and two stub registration calls;
   * "OpenGL\\OpenGL.h" and "thrust\\*.h": the reference includes these with
     Windows path separators; the shims forward to the real headers;
   * prelude.h (force-included): std::powf for libstdc++, and a forward
     declaration of CUDA::SafeCall that MSVC's permissive lookup did not need.
-The cubin is loaded on the GPU by oracle/ref_harness.cu, which build_harness()
-compiles on a machine with a GPU (the cubin travels; the checkout need not).
-Nothing here is run unless the reference checkout is present (cubin) or the
-cubin is (harness); outputs go only to oracle/_ref/.  write_input /
-read_output / time_reference_kernels drive the harness.
+The cubins are loaded on the GPU by oracle/ref_harness.cu (single scale) and
+oracle/ref_harness_ts.cu (two scale, coupled), which build_harness() compiles on
+a machine with a GPU (the cubins travel; the checkout need not).  Nothing here
+runs unless SPH2S_REFERENCE is set (cubins) or the cubins exist (harnesses);
+outputs go only to oracle/_ref/.
+
+  SPH2S_REFERENCE=<checkout> python -m oracle.ref_build      builds the cubins
+
 TEST INFRASTRUCTURE ONLY.
 """
 from __future__ import annotations
@@ -35,10 +41,24 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 SHIMS = OUT / "shims"
 CUBIN = OUT / "ss_solver.cubin"
+CUBIN_TS = OUT / "ts_solver.cubin"
+CUBIN_CP = OUT / "cp_solver.cubin"
 HARNESS = OUT / "ref_harness"
 HARNESS_CU = HERE / "ref_harness.cu"
-REFERENCE = Path(os.environ.get("SPH2S_REFERENCE", "/root/reference"))
-SOLVER_CU = REFERENCE / "SPH2S_FINAL_SINGLE_SCALE" / "Solver.cu"
+HARNESS_TS = OUT / "ref_harness_ts"
+HARNESS_TS_CU = HERE / "ref_harness_ts.cu"
+PROJECTS = {CUBIN: "SPH2S_FINAL_SINGLE_SCALE", CUBIN_TS: "SPH2S_FINAL_TWO_SCALE",
+            CUBIN_CP: "SPH2S_FINAL_TWO_SCALE_COUPLED"}
+
+
+def reference_root() -> Path | None:
+    r = os.environ.get("SPH2S_REFERENCE")
+    return Path(r) if r else None
+
+
+def solver_cu(cubin: Path) -> Path | None:
+    root = reference_root()
+    return None if root is None else root / PROJECTS[cubin] / "Solver.cu"
 
 SHIM_FILES = {
     "Windows.h": "",
@@ -64,43 +84,58 @@ SHIM_FILES = {
 
 
 def available() -> bool:
-    return SOLVER_CU.exists()
+    src = solver_cu(CUBIN)
+    return src is not None and src.exists()
 
 
-def build(force: bool = False) -> Path | None:
-    """Compiles the cubin when the reference checkout is present."""
+def build(force: bool = False) -> list[Path]:
+    """Compiles the three cubins when a reference checkout is configured."""
     if not available():
-        return CUBIN if CUBIN.exists() else None
-    if CUBIN.exists() and not force and CUBIN.stat().st_mtime > SOLVER_CU.stat().st_mtime:
-        return CUBIN
+        return [c for c in PROJECTS if c.exists()]
     SHIMS.mkdir(parents=True, exist_ok=True)
     for name, text in SHIM_FILES.items():
         (SHIMS / name).write_text(text)
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    tmp = CUBIN.with_suffix(".tmp")
-    cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-           "-I", str(SHIMS), "-include", str(SHIMS / "prelude.h"), str(SOLVER_CU), "-o", str(tmp)]
+    built = []
+    for cubin in PROJECTS:
+        src = solver_cu(cubin)
+        if cubin.exists() and not force and cubin.stat().st_mtime > src.stat().st_mtime:
+            built.append(cubin)
+            continue
+        tmp = cubin.with_suffix(".tmp")
+        cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+               "-I", str(SHIMS), "-include", str(SHIMS / "prelude.h"), str(src), "-o", str(tmp)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference kernels failed to build: {' '.join(cmd)}\n{r.stderr}")
+        os.replace(tmp, cubin)
+        built.append(cubin)
+    return built
+
+
+def _build_exe(src: Path, exe: Path) -> Path:
+    if exe.exists() and exe.stat().st_mtime > src.stat().st_mtime:
+        return exe
+    OUT.mkdir(parents=True, exist_ok=True)
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    tmp = exe.with_suffix(".tmp")
+    cmd = [nvcc, "-O2", "-gencode", "arch=compute_103a,code=sm_103a", str(src), "-o", str(tmp),
+           "-lcuda"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"reference kernels failed to build: {' '.join(cmd)}\n{r.stderr}")
-    os.replace(tmp, CUBIN)
-    return CUBIN
+        raise RuntimeError(f"{src.name} failed to build: {' '.join(cmd)}\n{r.stderr}")
+    os.replace(tmp, exe)
+    return exe
 
 
 def build_harness() -> Path:
     """Compiles oracle/ref_harness.cu for sm_103a (needs nvcc and libcuda)."""
-    if HARNESS.exists() and HARNESS.stat().st_mtime > HARNESS_CU.stat().st_mtime:
-        return HARNESS
-    OUT.mkdir(parents=True, exist_ok=True)
-    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    tmp = HARNESS.with_suffix(".tmp")
-    cmd = [nvcc, "-O2", "-gencode", "arch=compute_103a,code=sm_103a", str(HARNESS_CU),
-           "-o", str(tmp), "-lcuda"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"ref_harness failed to build: {' '.join(cmd)}\n{r.stderr}")
-    os.replace(tmp, HARNESS)
-    return HARNESS
+    return _build_exe(HARNESS_CU, HARNESS)
+
+
+def build_harness_ts() -> Path:
+    """Compiles oracle/ref_harness_ts.cu for sm_103a (needs nvcc and libcuda)."""
+    return _build_exe(HARNESS_TS_CU, HARNESS_TS)
 
 
 def write_input(path, config, x, v, boundary, steps: int, dt: float) -> None:
@@ -160,5 +195,115 @@ def time_reference_kernels(config, x, boundary, steps: int, dt: float, warmup: i
     return ms
 
 
+# ---- two-scale and coupled projects (oracle/ref_harness_ts.cu) ----------------
+
+MODE_BLENDED, MODE_COUPLED = 0, 1
+
+
+def ts_config_bytes(cfg, mode: int) -> bytes:
+    """SolverConfiguration of the two-scale project (TS Solver.h:52-61, 100 bytes)
+    or of the coupled one (CP Solver.h:50-58, 96 bytes: no BlendIncrement),
+    from an object with the sph_config2 field names."""
+    f = [cfg.effective_radius[0], cfg.effective_radius[1], cfg.fluid_particle_mass[0],
+         cfg.fluid_particle_mass[1], cfg.boundary_particle_mass, cfg.rest_density,
+         cfg.bulk_modulus, cfg.viscosity, cfg.speed_sound, cfg.tension_coefficient]
+    if mode == MODE_BLENDED:
+        f.append(cfg.blend_increment)
+    b = np.array(f, np.float32).tobytes()
+    for g in (cfg.grid[0], cfg.grid[1]):
+        b += np.array(list(g.origin), np.float32).tobytes()
+        b += np.array(list(g.dims), np.int32).tobytes()
+        b += np.array([g.spacing], np.float32).tobytes()
+    return b
+
+
+def write_input_ts(path, mode, cfg, pops, boundary, caps, steps: int, dt: float) -> None:
+    """pops = [low, high], each a dict of x (n,3), v (n,3), lam (n), state (n)."""
+    cb = ts_config_bytes(cfg, mode)
+    b = np.ascontiguousarray(boundary, np.float32).reshape(-1, 3)
+    n = [np.asarray(p["x"]).reshape(-1, 3).shape[0] for p in pops]
+    with open(path, "wb") as f:
+        f.write(b"SPHTSI01")
+        f.write(np.array([mode, len(cb)], np.uint32).tobytes())
+        f.write(cb)
+        f.write(np.array([n[0], n[1], b.shape[0], caps[0], caps[1], steps], np.uint32).tobytes())
+        f.write(np.array([dt], np.float32).tobytes())
+        for p, k in zip(pops, n):
+            f.write(np.ascontiguousarray(p["x"], np.float32).reshape(k, 3).tobytes())
+            f.write(np.ascontiguousarray(p["v"], np.float32).reshape(k, 3).tobytes())
+            f.write(np.ascontiguousarray(p["lam"], np.float32).reshape(k).tobytes())
+            f.write(np.ascontiguousarray(p["state"], np.int32).reshape(k).tobytes())
+        f.write(b.tobytes())
+
+
+def read_output_ts(path) -> list[dict]:
+    """Per recorded step: {"fields": [low, high], "post": [low, high],
+    "high_survivors", "slot_overlap"}.  fields[r]: sorted order of the step's
+    force pass (pid, hash, rho, p, acc, colour, state, lam); post[r]: the
+    particles listed active after the step, in list order (pid, x, v, state,
+    lam)."""
+    raw = Path(path).read_bytes()
+    assert raw[:8] == b"SPHTSO01"
+    off = 8
+
+    def take(dt, count):
+        nonlocal off
+        a = np.frombuffer(raw, dt, count=int(count), offset=off).copy()
+        off += a.nbytes
+        return a
+
+    mode, rec = take(np.uint32, 2)
+    steps = []
+    for _ in range(int(rec)):
+        fields = []
+        for _r in range(2):
+            n = int(take(np.uint32, 1)[0])
+            fields.append({"pid": take(np.uint32, n), "hash": take(np.uint32, n),
+                           "rho": take(np.float32, n), "p": take(np.float32, n),
+                           "acc": take(np.float32, 3 * n).reshape(n, 3),
+                           "colour": take(np.float32, n), "state": take(np.int32, n),
+                           "lam": take(np.float32, n)})
+        post = []
+        for _r in range(2):
+            count, slots = (int(v) for v in take(np.uint32, 2))
+            active = take(np.uint32, count).astype(np.int64)
+            x = take(np.float32, 3 * slots).reshape(slots, 3)
+            v = take(np.float32, 3 * slots).reshape(slots, 3)
+            st = take(np.int32, slots)
+            lam = take(np.float32, slots)
+            pid = take(np.uint32, slots)
+            post.append({"pid": pid[active], "x": x[active], "v": v[active],
+                         "state": st[active], "lam": lam[active]})
+        hs, ov = (int(v) for v in take(np.uint32, 2))
+        steps.append({"fields": fields, "post": post, "high_survivors": hs, "slot_overlap": ov})
+    return steps
+
+
+def run_harness_ts(mode, cfg, pops, boundary, caps, steps: int, dt: float,
+                   warmup: int | None = None):
+    """Runs the reference's two-scale (mode 0) or coupled (mode 1) kernels;
+    returns (recorded steps, ms per timed step or None, end counts or None)."""
+    cubin = CUBIN_TS if mode == MODE_BLENDED else CUBIN_CP
+    if not cubin.exists():
+        raise FileNotFoundError(f"{cubin} is missing (built where the reference checkout is)")
+    exe = build_harness_ts()
+    with tempfile.TemporaryDirectory() as tmp:
+        fin, fout = Path(tmp) / "in.bin", Path(tmp) / "out.bin"
+        write_input_ts(fin, mode, cfg, pops, boundary, caps, steps, dt)
+        cmd = [str(exe), str(cubin), str(fin), str(fout)]
+        if warmup is not None:
+            cmd += ["--time", str(int(warmup))]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_harness_ts failed ({r.returncode}): {r.stderr.strip()}")
+        m = re.search(r"ref_harness_ms_per_step\s+([0-9.eE+-]+)", r.stdout)
+        c = re.search(r"ref_harness_counts\s+(\d+)\s+(\d+)", r.stdout)
+        return (read_output_ts(fout), float(m.group(1)) if m else None,
+                (int(c.group(1)), int(c.group(2))) if c else None)
+
+
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    if not available():
+        sys.exit("set SPH2S_REFERENCE to the reference checkout")
+    for c in build(force="--force" in sys.argv):
+        print(c)

@@ -1,8 +1,8 @@
-"""In-tree build of libsph2s.so (nvcc, sm_103a only) and of the CPU oracle.
+"""In-tree build of libsph2s.so (nvcc, sm_103a only).
 
 The translation units are compiled in parallel and linked with nvcc; nothing is
 installed outside the repository.  `python -m sph2s_final_gb300.build` builds
-both libraries.
+the library.
 """
 from __future__ import annotations
 
@@ -18,8 +18,6 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libsph2s.so"
-ORACLE_DIR = ROOT / "oracle"
-ORACLE_LIB = ROOT / "oracle" / "_build" / "liboracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -92,30 +90,8 @@ def build_library(force: bool = False, verbose: bool = False, ptxas_v: bool = Fa
     return LIB
 
 
-def build_oracle(force: bool = False) -> Path:
-    """Builds the CPU oracle (test infrastructure only)."""
-    srcs = sorted(ORACLE_DIR.glob("*.cpp"))
-    if not force and not _stale(ORACLE_LIB, srcs + list(ORACLE_DIR.glob("*.h"))):
-        return ORACLE_LIB
-    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    cxx = os.environ.get("CXX", "g++")
-    tmp = ORACLE_LIB.with_suffix(".so.tmp")
-    cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           *map(str, srcs), "-o", str(tmp)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
-
-
 def main() -> None:
-    force = "--force" in sys.argv
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        a = ex.submit(build_library, force, "--verbose" in sys.argv, "--ptxas" in sys.argv)
-        b = ex.submit(build_oracle, force)
-        print(a.result())
-        print(b.result())
+    print(build_library("--force" in sys.argv, "--verbose" in sys.argv, "--ptxas" in sys.argv))
 
 
 if __name__ == "__main__":

@@ -16,7 +16,8 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def _built():
     """Builds libsph2s.so and the oracle in-tree once per session."""
-    from sph2s_final_gb300.build import build_library, build_oracle
+    from oracle.build import build_oracle
+    from sph2s_final_gb300.build import build_library
     build_library()
     build_oracle()
     yield
