@@ -117,6 +117,17 @@ int sph_get_densities(sph_solver* s, float* rho, int32_t order);
  * until sph_sync; at most two readbacks are in flight (a third waits for the
  * first). */
 int sph_get_positions_async(sph_solver* s, float* xyz, int32_t order);
+/* Device-resident readback (the reference's own consumers read
+ * ParticleData::dPositions in device memory every frame, the renderer through
+ * the mapped VBO, SPH2S_FINAL_SINGLE_SCALE/ParticleData.cpp:47-66,
+ * main.cpp:79): the same arrays as sph_get_positions / _velocities /
+ * _densities, written into caller-owned device memory (3 floats per particle,
+ * 1 for densities) by a kernel on the handle's stream.  Asynchronous: order
+ * later work after sph_stream(s) or call sph_sync.  A destination that is not
+ * device or managed memory of the current device: SPH_E_INVALID. */
+int sph_get_positions_device(sph_solver* s, float* d_xyz, int32_t order);
+int sph_get_velocities_device(sph_solver* s, float* d_xyz, int32_t order);
+int sph_get_densities_device(sph_solver* s, float* d_rho, int32_t order);
 /* Persistent ids in sorted order (ids[k] = input index of the k-th particle). */
 int sph_get_ids(sph_solver* s, uint32_t* ids);
 /* Overwrites the velocities (3 floats per particle) in the given order. */
@@ -299,6 +310,12 @@ int sph2_last_stats(sph_solver2* s, uint32_t* stats6);
  * group ids (0xFFFFFFFF = none) and persistent ids. */
 int sph2_get_state(sph_solver2* s, int32_t population, float* xyz, float* vel, float* lambda,
                    int32_t* state, uint32_t* group, uint32_t* ids);
+/* Positions of one population in its current order (3 floats per particle)
+ * written into caller-owned device memory by a kernel on the handle's stream,
+ * as sph_get_positions_device: the two-scale renderer's read of
+ * ParticleData::dPositions (SPH2S_FINAL_TWO_SCALE/ParticleData.h:38-43).
+ * Asynchronous; a destination that is not device memory: SPH_E_INVALID. */
+int sph2_get_positions_device(sph_solver2* s, int32_t population, float* d_xyz);
 /* Parity instrumentation: for the current state, without advancing, the
  * sorted persistent ids, densities, accelerations and neighbour counts (same
  * population, complementary population, boundary) of one population, in the
@@ -397,15 +414,16 @@ int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* k
 
 /* sph_sort_pairs for callers that cannot allocate device memory (no
  * counterpart in the reference): hosts that own a fixed device-memory budget
- * and pass only their own buffers, code running while a global-mode stream
- * capture is open elsewhere (cudaMalloc is illegal then), or loops that must
- * not risk an allocation's implicit synchronisation.  Same arguments and
- * results as sph_sort_pairs; calls no cudaMalloc/cudaFree.  Its scratch is one
- * static device array of about 10 MB that each GPU loading the library holds
- * until exit, which limits n to 1,048,576 pairs (larger n: SPH_E_CAPACITY).
- * The first call on a device looks the array up (make it before any stream
- * capture); all calls share the array, so calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * and pass only their own buffers (an engine whose memory manager owns every
+ * device allocation), or loops that must not risk an allocation's implicit
+ * synchronisation.  Same arguments and results as sph_sort_pairs; calls no
+ * cudaMalloc/cudaFree.  Its scratch is one static device array of about 10 MB
+ * that each GPU loading the library holds until exit, which limits n to
+ * 1,048,576 pairs (larger n: SPH_E_CAPACITY).  The first call on a device
+ * looks the array up (make it before any stream capture; the lookup is
+ * repeated after the device's context is recreated); all calls share the
+ * array, so calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                            uint32_t* vals_out, uint32_t n, int32_t key_bits, void* stream);
 

@@ -17,6 +17,9 @@ void set_last_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 // Maps a CUDA status to SPH_OK / SPH_E_CUDA, recording where it happened.
 int check_cuda(cudaError_t e, const char* what, const char* file, int line);
+// SPH_OK if p is device (or managed) memory usable on the current device; a
+// host pointer handed to a kernel would fault, so device readback checks first.
+int check_device_pointer(const void* p, const char* who);
 
 }  // namespace sph
 

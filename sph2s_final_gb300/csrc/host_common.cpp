@@ -28,6 +28,23 @@ int check_cuda(cudaError_t e, const char* what, const char* file, int line) {
     return SPH_E_CUDA;
 }
 
+int check_device_pointer(const void* p, const char* who) {
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SPH_E_INVALID, std::string(who) + ": not a CUDA pointer");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        return fail(SPH_E_INVALID, std::string(who) + ": destination is not device memory");
+    int dev = -1;
+    int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice", __FILE__, __LINE__);
+    if (rc != SPH_OK) return rc;
+    if (a.type == cudaMemoryTypeDevice && a.device != dev)
+        return fail(SPH_E_INVALID, std::string(who) + ": destination is on another device");
+    return SPH_OK;
+}
+
 }  // namespace sph
 
 using sph::fail;

@@ -187,14 +187,6 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
-size_t sort_scratch_bytes(uint32_t max_n) {
-    uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
-    if (tiles == 0) tiles = 1;
-    size_t b = align256(kSortMaxPasses * 256 * 4) + align256(kSortMaxPasses * 4) +
-               align256((size_t)kSortMaxPasses * tiles * 256 * 4);
-    return b;
-}
-
 SortScratch sort_scratch_from(void* base, uint32_t max_n) {
     SortScratch s;
     uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;

@@ -38,8 +38,15 @@ struct SortScratch {
     size_t zero_bytes;   // bytes from hist through status
 };
 
-// Bytes of scratch a plan for up to max_n keys needs.
-size_t sort_scratch_bytes(uint32_t max_n);
+constexpr size_t sort_align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bytes of scratch a plan for up to max_n keys needs (a constant expression, so
+// fixed-size scratch regions can be checked at build time).
+constexpr size_t sort_scratch_bytes(uint32_t max_n) {
+    return sort_align256(kSortMaxPasses * 256 * 4) + sort_align256(kSortMaxPasses * 4) +
+           sort_align256((size_t)kSortMaxPasses *
+                         (max_n == 0 ? 1u : (max_n + kSortTile - 1) / kSortTile) * 256 * 4);
+}
 // Carves a SortScratch out of a caller-provided device block of
 // sort_scratch_bytes(max_n) bytes (256-byte aligned).
 SortScratch sort_scratch_from(void* base, uint32_t max_n);

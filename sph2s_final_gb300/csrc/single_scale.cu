@@ -404,6 +404,45 @@ int sph_get_densities(sph_solver* s, float* rho, int32_t order) {
     return SPH_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+int device_readback(sph_solver* s, const float4* src4, const float* src1, void* dst, int32_t order,
+                    const char* who) {
+    if (!s || (!dst && s->n)) return fail(SPH_E_INVALID, std::string(who) + ": NULL argument");
+    if (order != SPH_ORDER_SORTED && order != SPH_ORDER_BY_ID) return fail(SPH_E_INVALID, "bad order");
+    if (s->n == 0) return SPH_OK;
+    int rc = check_device_pointer(dst, who);
+    if (rc != SPH_OK) return rc;
+    if (src4)
+        pack_xyz_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(src4, s->pos, s->n,
+                                                                 order == SPH_ORDER_BY_ID,
+                                                                 static_cast<float*>(dst));
+    else
+        pack_scalar_kernel<<<blocks_for(s->n), 256, 0, s->stream>>>(src1, s->pos, s->n,
+                                                                    order == SPH_ORDER_BY_ID,
+                                                                    static_cast<float*>(dst));
+    SPH_CUDA(cudaGetLastError());
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_get_positions_device(sph_solver* s, float* d_xyz, int32_t order) {
+    return device_readback(s, s ? s->pos : nullptr, nullptr, d_xyz, order, "sph_get_positions_device");
+}
+
+int sph_get_velocities_device(sph_solver* s, float* d_xyz, int32_t order) {
+    return device_readback(s, s ? s->vel : nullptr, nullptr, d_xyz, order, "sph_get_velocities_device");
+}
+
+int sph_get_densities_device(sph_solver* s, float* d_rho, int32_t order) {
+    return device_readback(s, nullptr, s ? s->rho : nullptr, d_rho, order, "sph_get_densities_device");
+}
+
 int sph_get_ids(sph_solver* s, uint32_t* ids) {
     if (!s || (!ids && s->n)) return fail(SPH_E_INVALID, "sph_get_ids: NULL argument");
     int rc = sph_sync(s);

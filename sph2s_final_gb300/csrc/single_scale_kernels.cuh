@@ -120,6 +120,21 @@ static __global__ void __launch_bounds__(256) pack_xyz_kernel(const float4* __re
     dst[3 * (size_t)d + 2] = v.z;
 }
 
+// Scalar field (one float per particle) into a caller's array, in sorted order
+// or scattered by the persistent ids in ids[k].w.
+static __global__ void __launch_bounds__(256) pack_scalar_kernel(const float* __restrict__ src,
+                                                         const float4* __restrict__ ids, uint32_t n,
+                                                         int by_id, float* __restrict__ dst) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t d = k;
+    if (by_id) {
+        d = __float_as_uint(ids[k].w);
+        if (d >= n) return;
+    }
+    dst[d] = src[k];
+}
+
 // Per-cell flag: does any boundary particle lie within `reach` cells of this
 // cell?  A particle's stencil [cell(x-h), cell(x+h)] never leaves
 // cell(x) +- (ceil(h/spacing) + 1), so particles in cells without the flag

@@ -628,6 +628,19 @@ int sph2_get_state(sph_solver2* s, int32_t population, float* xyz, float* vel, f
     return SPH_OK;
 }
 
+int sph2_get_positions_device(sph_solver2* s, int32_t population, float* d_xyz) {
+    if (!s || population < 0 || population > 1)
+        return fail(SPH_E_INVALID, "sph2_get_positions_device: bad handle or population");
+    Pop& p = s->pop[population];
+    if (p.n == 0) return SPH_OK;
+    if (!d_xyz) return fail(SPH_E_INVALID, "sph2_get_positions_device: NULL destination");
+    int rc = sph::check_device_pointer(d_xyz, "sph2_get_positions_device");
+    if (rc != SPH_OK) return rc;
+    pack_xyz_kernel<<<blocks_for(p.n), 256, 0, s->stream>>>(p.pos, p.pos, p.n, 0, d_xyz);
+    SPH_CUDA(cudaGetLastError());
+    return SPH_OK;
+}
+
 int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sorted, float* rho,
                            float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
                            uint32_t* nbr_boundary) {

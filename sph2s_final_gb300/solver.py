@@ -174,6 +174,15 @@ class Solver:
         check(lib().sph_get_densities(self._h, fptr(out), ORDER[order]))
         return out
 
+    def read_device(self, field: str, device_ptr: int, order: str = "sorted") -> None:
+        """Enqueues a copy of "positions", "velocities" (3 floats per particle)
+        or "densities" into caller-owned device memory at `device_ptr`, on the
+        solver's stream (order later work after `stream` or call sync())."""
+        fn = {"positions": lib().sph_get_positions_device,
+              "velocities": lib().sph_get_velocities_device,
+              "densities": lib().sph_get_densities_device}[field]
+        check(fn(self._h, C.c_void_p(device_ptr), ORDER[order]))
+
     def ids(self) -> np.ndarray:
         out = np.empty(self.num_fluid, np.uint32)
         check(lib().sph_get_ids(self._h, uptr(out)))

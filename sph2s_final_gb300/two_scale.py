@@ -103,6 +103,11 @@ class Solver2:
                                    uptr(r["group"]), uptr(r["ids"])))
         return r
 
+    def read_positions_device(self, population: int, device_ptr: int) -> None:
+        """Enqueues a copy of one population's positions (current order, 3 floats
+        per particle) into caller-owned device memory on the solver's stream."""
+        check(lib().sph2_get_positions_device(self._h, population, C.c_void_p(device_ptr)))
+
     def debug_step_fields(self, population: int) -> dict:
         n = self.counts()["low" if population == LOW else "high"]
         r = {"ids": np.empty(n, np.uint32), "rho": np.empty(n, np.float32),

@@ -1,7 +1,10 @@
 """The C ABI from compiled code: tests/cabi_client.cpp and tests/cabi_client2.cpp
 are the reference-side adapters (the single-scale and two-scale `Solver`
 classes that forward to include/sph2s.h), each driving a scene built with the
-ABI's grid, particle-box and configuration builders.
+ABI's grid, particle-box and configuration builders; tests/cabi_client3.cpp is
+the reference's own host-program flow (initSim / display) on the header-only
+drop-in include/sph2s_solver.hpp (Grid, SolverConfiguration, ParticleData with
+device arrays, Solver(ParticleData*, ParticleData*, const SolverConfiguration*)).
 
 CPU: the header compiles as C99 and as C++17 with warnings as errors, and both
 clients link against libsph2s.so.  GPU: each client's run equals the same run
@@ -30,12 +33,20 @@ def compiler(name):
     return exe
 
 
+CUDA_HOME = Path("/usr/local/cuda")
+
+
 def build_client(tmp_path, name="cabi_client"):
     _abi.lib()  # the library is built (raises with the build command otherwise)
     exe = tmp_path / name
     cmd = [compiler("g++"), "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
            "-I", str(ROOT / "include"), str(ROOT / "tests" / f"{name}.cpp"),
            "-L", str(PKG), "-lsph2s", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
+    if name == "cabi_client3":  # the drop-in header allocates ParticleData with the CUDA runtime
+        if not (CUDA_HOME / "include" / "cuda_runtime.h").exists():
+            pytest.skip("CUDA runtime headers not found")
+        cmd[-2:-2] = ["-isystem", str(CUDA_HOME / "include"), "-L", str(CUDA_HOME / "lib64"),
+                      "-lcudart", f"-Wl,-rpath,{CUDA_HOME / 'lib64'}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
@@ -50,7 +61,7 @@ def test_header_compiles_as_c(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.parametrize("name", ["cabi_client", "cabi_client2"])
+@pytest.mark.parametrize("name", ["cabi_client", "cabi_client2", "cabi_client3"])
 def test_client_compiles_and_links(tmp_path, name):
     assert build_client(tmp_path, name).exists()
 
@@ -137,3 +148,40 @@ def test_two_scale_client_run_equals_python_binding(tmp_path):
             for k in ("ids", "x", "v", "lam", "state", "group"):
                 np.testing.assert_array_equal(st[k], pops[pop][k], err_msg=f"{pop} {k}")
     assert np.isfinite(pops[LOW]["x"]).all() and np.isfinite(pops[HIGH]["x"]).all()
+
+
+def read_run3(path):
+    data = path.read_bytes()
+    nf, nb, steps = struct.unpack_from("<III", data, 0)
+    (dt,) = struct.unpack_from("<f", data, 12)
+    off = 16
+    cfg = _abi.sph_config.from_buffer_copy(data, off)
+    off += C.sizeof(_abi.sph_config)
+    fluid = np.frombuffer(data, np.float32, 3 * nf, off).reshape(nf, 3).copy()
+    off += 12 * nf
+    boundary = np.frombuffer(data, np.float32, 3 * nb, off).reshape(nb, 3).copy()
+    off += 12 * nb
+    x = np.frombuffer(data, np.float32, 3 * nf, off).reshape(nf, 3).copy()
+    off += 12 * nf
+    ids = np.frombuffer(data, np.uint32, nf, off).copy()
+    off += 4 * nf
+    assert off == len(data)
+    return cfg, fluid, boundary, steps, dt, x, ids
+
+
+@pytest.mark.gpu
+def test_reference_host_flow_on_the_drop_in_header(tmp_path):
+    """initSim / display through include/sph2s_solver.hpp: the positions the
+    Solver writes into the fluid ParticleData's device array every Advance are
+    the Python binding's sorted positions, bit for bit."""
+    exe = build_client(tmp_path, "cabi_client3")
+    out = tmp_path / "run3.bin"
+    r = subprocess.run([str(exe), str(out), "20"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cfg, fluid, boundary, steps, dt, x, ids = read_run3(out)
+    assert steps == 20 and fluid.shape[0] > 10000 and boundary.shape[0] > 100000
+    with Solver(ParticleData(fluid), ParticleData(boundary), cfg) as s:
+        s.advance(dt, steps)
+        np.testing.assert_array_equal(s.ids(), ids)
+        np.testing.assert_array_equal(s.positions("sorted"), x)
+    assert np.abs(x[np.argsort(ids)] - fluid).max() > 0  # the client did step the scene
