@@ -10,9 +10,24 @@ boundary particles, 128^3 cells, dt 2.5e-5), 100 warm-up + 1,000 timed steps.
 HBM); `e2e` goes through the public API (sph_create from host arrays, then per
 step sph_advance + a device->host read of the positions into pinned memory).
 `--impl reference` times the CPU restatement of the reference step (the
-reference has no CPU path of its own and its CUDA 5.0/OpenGL build cannot run
-here) on the host cores.  With N > 1 each rank runs an independent replica
-(the path does not shard; there is no collective).
+reference has no CPU path of its own and its CUDA 5.0/OpenGL program cannot
+run here) on the host cores, and beside it the reference's own step kernels
+rebuilt for this GPU (`reference_gpu`); that arm builds its scene with
+oracle/scenes_ref.py and loads nothing of the product.  With N > 1 each rank
+runs an independent replica (the path does not shard; there is no collective).
+
+Roofline arithmetic (density and force passes, per launch):
+  bytes  density 16 + 4 + 8 C/N B per particle (positions in, density out,
+         cell table); force + integrate 72 + 16 C/N + 16 B_touched/N
+  flops  density 8 per candidate (3 sub, r^2 as mul + 2 fma) + 4 per neighbour
+         (Poly6 (h^2-r^2)^3 accumulated); force 38 per fluid neighbour
+         (distance, rsqrt, spiky, Laplacian, Poly6 tension, 2 x 3 fma) + 16 per
+         boundary neighbour; fma counted as 2.  Candidates (particles in the
+         stencil cells) and neighbours are counted exactly for the timed
+         state: candidates by a summed-area table of the cell occupancy in
+         numpy, neighbours from the solver's own debug pass.
+  peaks  HBM: MEASURED_PEAKS.json hbm_gbs; FP32: SMs x 128 lanes x 2 x the
+         SM clock sampled during the timed region.
 """
 from __future__ import annotations
 
@@ -51,20 +66,49 @@ def parse_args():
     return ap.parse_args()
 
 
+WORKLOADS = {
+    "c1": (1 / 256, "dam break 2,097,152 fluid + 2,043,880 boundary, s=1/256, h=2s, 128^3 cells, "
+                    "dt=2.5e-5"),
+    "c0": (1 / 64, "dam break 32,768 fluid + 143,080 boundary, s=1/64, h=2s, 32^3 cells, dt=1e-4"),
+}
+
+
 def workload(name: str):
+    """The product's scene builders (libsph2s.so)."""
     from sph2s_final_gb300 import scenes
-    if name == "c1":
-        sc = scenes.dam_break(1 / 256)
-        desc = "dam break 2,097,152 fluid + 2,043,880 boundary, s=1/256, h=2s, 128^3 cells, dt=2.5e-5"
-    else:
-        sc = scenes.dam_break(1 / 64)
-        desc = "dam break 32,768 fluid + 143,080 boundary, s=1/64, h=2s, 32^3 cells, dt=1e-4"
+    spacing, desc = WORKLOADS[name]
+    return scenes.dam_break(spacing), desc
+
+
+def workload_reference(name: str):
+    """The same scene restated in numpy (byte-identical, tests/test_scenes_ref.py),
+    so the reference arm loads nothing of the product."""
+    from oracle import scenes_ref
+    spacing, desc = WORKLOADS[name]
+    r = scenes_ref.dam_break(spacing)
+
+    class _P:  # ParticleData-like view
+        def __init__(self, a):
+            self.positions = a
+            self.num_particles = int(a.shape[0])
+
+    class _S:
+        pass
+    sc = _S()
+    sc.fluid, sc.boundary, sc.config, sc.dt, sc.spacing = _P(r.fluid), _P(r.boundary), r.config, r.dt, r.spacing
     return sc, desc
 
 
+def config_for(desc: str, ws: int) -> dict:
+    """The `config` object of both arms' lines."""
+    return {"workload": desc, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            "l2": "working set ~0.3 GB > 129 MB L2 (no flush needed)"}
+
+
 def dist_env():
-    from sph2s_final_gb300 import replicas
-    return replicas.world()
+    """(world size, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def physical_gpu_index(local: int) -> str:
@@ -140,9 +184,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic(kernel: str, wl: str):
-    """Per-launch DRAM bytes of `kernel` on workload `wl` from the committed ncu summaries."""
-    pat = re.compile(rf"traffic_bytes_per_launch:\s*{re.escape(kernel)}\s+{wl}\s+([0-9.eE+]+)")
+def committed_metric(name: str, kernel: str, wl: str):
+    """A per-launch figure `name` of `kernel` on workload `wl` from the committed
+    ncu summaries under profiles/ (lines "name: kernel wl value")."""
+    pat = re.compile(rf"{re.escape(name)}:\s*{re.escape(kernel)}\s+{wl}\s+([0-9.eE+]+)")
     for f in sorted((ROOT / "profiles").glob("*.md")):
         m = pat.search(f.read_text())
         if m:
@@ -150,24 +195,98 @@ def committed_traffic(kernel: str, wl: str):
     return None
 
 
+def _cell_coord(x, o, s, d, off=0.0):
+    """clamp(trunc(((x + off) - o) / s), 0, d - 1) in FP32, as the kernels."""
+    t = (x.astype(np.float32) + np.float32(off)) - np.float32(o)
+    t = t / np.float32(s)
+    t = np.clip(t, np.float32(-1.0), np.float32(d))
+    return np.clip(np.trunc(t).astype(np.int64), 0, d - 1)
+
+
+def stencil_candidates(grid, h, query, source):
+    """Per query particle: source particles in the cells of its stencil
+    [cell(x - h), cell(x + h)] (self included), by a summed-area table."""
+    d = [int(v) for v in grid.dims]
+    o = [float(v) for v in grid.origin]
+    s = float(grid.spacing)
+    src = np.asarray(source, np.float32)
+    cx, cy, cz = (_cell_coord(src[:, a], o[a], s, d[a]) for a in range(3))
+    occ = np.zeros((d[2] + 1, d[1] + 1, d[0] + 1), np.int64)
+    np.add.at(occ, (cz + 1, cy + 1, cx + 1), 1)
+    sat = occ.cumsum(0).cumsum(1).cumsum(2)
+    q = np.asarray(query, np.float32)
+    lo = [_cell_coord(q[:, a], o[a], s, d[a], -h) for a in range(3)]
+    hi = [_cell_coord(q[:, a], o[a], s, d[a], h) + 1 for a in range(3)]
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    return (sat[z1, y1, x1] - sat[z0, y1, x1] - sat[z1, y0, x1] - sat[z1, y1, x0]
+            + sat[z0, y0, x1] + sat[z0, y1, x0] + sat[z1, y0, x0] - sat[z0, y0, x0])
+
+
 def boundary_touched(sc) -> int:
-    """Boundary particles within one cell (Chebyshev) of a fluid-occupied cell."""
-    from oracle import oracle as O  # host-side counting only
+    """Boundary particles in a cell that the stencil of some fluid particle covers."""
     g = sc.config.grid
-    _, lf = O.cell_keys(g, sc.fluid.positions)
-    _, lb = O.cell_keys(g, sc.boundary.positions)
-    d = np.array(g.dims[:])
-    occ = np.zeros(d[::-1], bool)
-    cz, rem = np.divmod(lf, d[0] * d[1])
-    cy, cx = np.divmod(rem, d[0])
-    occ[cz, cy, cx] = True
-    dil = occ.copy()
-    for ax in range(3):
-        for sh in (-1, 1):
-            dil |= np.roll(occ, sh, axis=ax)  # roll wraps, but edges are clamped cells anyway
-    bz, rem = np.divmod(lb, d[0] * d[1])
-    by, bx = np.divmod(rem, d[0])
-    return int(dil[bz, by, bx].sum())
+    d = [int(v) for v in g.dims]
+    o = [float(v) for v in g.origin]
+    h = float(sc.config.effective_radius)
+    f = np.asarray(sc.fluid.positions, np.float32)
+    cover = np.zeros((d[2], d[1], d[0]), bool)
+    lo = [_cell_coord(f[:, a], o[a], float(g.spacing), d[a], -h) for a in range(3)]
+    hi = [_cell_coord(f[:, a], o[a], float(g.spacing), d[a], h) for a in range(3)]
+    for dz in range(3):
+        for dy in range(3):
+            for dx in range(3):
+                cover[np.minimum(lo[2] + dz, hi[2]), np.minimum(lo[1] + dy, hi[1]),
+                      np.minimum(lo[0] + dx, hi[0])] = True
+    b = np.asarray(sc.boundary.positions, np.float32)
+    bc = [_cell_coord(b[:, a], o[a], float(g.spacing), d[a]) for a in range(3)]
+    return int(cover[bc[2], bc[1], bc[0]].sum())
+
+
+FLOPS_DENS_CAND, FLOPS_DENS_NBR = 8, 4
+FLOPS_FORCE_NBR, FLOPS_FORCE_BND = 38, 16
+
+
+def step_work(scene_list, positions=None, nbr_per_candidate=None):
+    """Whole single-scale steps of a list of scenes: algorithmic bytes
+    (192 + 16 P) n + 40 C + 16 B_touched per scene (hash 24, sort 4 + 16 P with
+    P = 3 digit passes, reorder + cell table 72 n + 16 C, density 20 n + 8 C,
+    force + integrate 72 n + 16 C + 16 B_touched) and FP32 flops from exact
+    candidate counts; neighbours per candidate are the measured ratio of the
+    2M-particle step when given (the batch has no per-scene debug pass)."""
+    algo, flops = 0, 0
+    for k, sc in enumerate(scene_list):
+        x = sc.fluid.positions if positions is None else positions[k]
+        n = len(x)
+        cells = int(np.prod(list(sc.config.grid.dims)))
+        algo += 240 * n + 40 * cells + 16 * boundary_touched(sc)
+        cand = int(stencil_candidates(sc.config.grid, float(sc.config.effective_radius), x, x).sum())
+        ratio = nbr_per_candidate or 0.155
+        nbr = cand * ratio
+        flops += FLOPS_DENS_CAND * cand + FLOPS_DENS_NBR * nbr + FLOPS_FORCE_NBR * (nbr - n)
+    return algo, flops
+
+
+def fp32_peak_tflops(sm_mhz):
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, sms, mhz
+
+
+def pass_roofline(name, ms, algo_bytes, flops, peak_gbs, peak_kind, peak_tf, sms, mhz, wl):
+    gbs = algo_bytes / (ms * 1e-3) / 1e9
+    tf = flops / (ms * 1e-3) / 1e12
+    fb, ff = gbs / peak_gbs, tf / peak_tf
+    out = {"ms": ms, "algorithmic_bytes_per_launch": int(algo_bytes), "achieved_gbs": gbs,
+           "hbm_frac": fb, "flops_per_launch": int(flops), "achieved_tflops": tf,
+           "fp32_peak_tflops": peak_tf, "fp32_frac": ff,
+           "binds": "fp32 issue" if ff >= fb else "hbm",
+           "traffic": committed_metric("traffic_bytes_per_launch", name, wl),
+           "issue_active_pct": committed_metric("issue_active_pct", name, wl),
+           "peaks": f"HBM {peak_gbs:.0f} GB/s ({peak_kind}); FP32 {sms} SMs x 128 x 2 x "
+                    f"{mhz:.0f} MHz (sampled)"}
+    return out
 
 
 def cpu_baseline(sc, seconds: float):
@@ -188,7 +307,24 @@ def cpu_baseline(sc, seconds: float):
             "sample": f"FP64 oracle (C++/OpenMP) on the same scene, {steps} steps after 1 warm-up step"}
 
 
-def measure_batched(steps: int, warmup: int = 3):
+def cpu_baseline_c0(steps: int = 1000):
+    """The FP64 oracle over the whole 1,000-step 32,768-particle case on the host cores."""
+    from oracle import oracle as O
+    from sph2s_final_gb300 import scenes
+    sc = scenes.dam_break(1 / 64)
+    O.set_threads(os.cpu_count() or 1)
+    ro = O.SSRollout(sc.config, sc.fluid.positions, sc.boundary.positions)
+    t0 = time.perf_counter()
+    ro.advance(sc.dt, steps)
+    el = time.perf_counter() - t0
+    ro.close()
+    n = sc.fluid.num_particles
+    return {"value": n * steps / el, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "seconds": el, "sample": f"FP64 oracle, dam break 32,768 fluid + 143,080 boundary, "
+                                     f"all {steps} steps at dt 1e-4"}
+
+
+def measure_batched(steps: int, warmup: int = 3, peaks=None, ratio=None):
     """256 independent scenes (9.4M fluid particles): one batch stepped with one
     launch per kernel per step, against the same scenes stepped one after
     another by per-scene solvers (each with its own CUDA graph)."""
@@ -225,19 +361,29 @@ def measure_batched(steps: int, warmup: int = 3):
         s.advance(dt, steps)
         s.sync()
     serial_ms = 1e3 * (time.perf_counter() - t0)
+    xs = [s.positions() for s in solvers]
     for s in solvers:
         s.close()
-    return {"scenes": len(scs), "fluid_particles": n, "steps": steps, "dt": dt,
-            "batched_ms": batched_ms, "per_scene_serial_ms": serial_ms,
-            "speedup": serial_ms / batched_ms,
-            "batched_particle_steps_per_s": n * steps / (batched_ms * 1e-3),
-            "per_scene_particle_steps_per_s": n * steps / (serial_ms * 1e-3),
-            "autotune": choice,
-            "timing": "batched: CUDA events on the batch stream; per-scene: host clock, "
-                      "each scene synchronised before the next starts"}
+    out = {"scenes": len(scs), "fluid_particles": n, "steps": steps, "dt": dt,
+           "batched_ms": batched_ms, "per_scene_serial_ms": serial_ms,
+           "speedup": serial_ms / batched_ms,
+           "batched_particle_steps_per_s": n * steps / (batched_ms * 1e-3),
+           "per_scene_particle_steps_per_s": n * steps / (serial_ms * 1e-3),
+           "autotune": choice,
+           "timing": "batched: CUDA events on the batch stream; per-scene: host clock, "
+                     "each scene synchronised before the next starts"}
+    if peaks is not None:
+        algo, flops = step_work(scs, xs, ratio)
+        out["roofline"] = pass_roofline("batched_step", batched_ms / steps, algo, flops, *peaks,
+                                        "c4")
+        out["roofline"]["note"] = ("whole batched step; bytes by the single-scale per-pass "
+                                   "formulas summed over the scenes; flops from exact candidate "
+                                   "counts of the final state, neighbours at the 2M step's "
+                                   "measured neighbours per candidate")
+    return out
 
 
-def measure_adjoint(steps: int = 200, every: int = 20, reps: int = 3):
+def measure_adjoint(steps: int = 200, every: int = 20, reps: int = 3, peaks=None, ratio=None):
     """65,536-particle differentiable rollout (T steps, checkpoints every K):
     forward (with checkpoints) and backward (segment recompute + adjoint
     kernels) wall time per rollout, synchronous calls, best of `reps`."""
@@ -269,11 +415,27 @@ def measure_adjoint(steps: int = 200, every: int = 20, reps: int = 3):
             s.advance(sc.dt, steps)
             s.sync()
             plain.append(time.perf_counter() - t4)
+        xs = [s.positions()]
     f, b, p = min(fw), min(bw), min(plain)
-    return {"particles": sc.fluid.num_particles, "steps": steps, "checkpoint_every": every,
-            "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "plain_forward_ms": 1e3 * p,
-            "adjoint_over_forward": b / f, "adjoint_over_plain_forward": b / p,
-            "loss": loss, "timing": "host clock around synchronous calls, best of 3"}
+    out = {"particles": sc.fluid.num_particles, "steps": steps, "checkpoint_every": every,
+           "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "plain_forward_ms": 1e3 * p,
+           "adjoint_over_forward": b / f, "adjoint_over_plain_forward": b / p,
+           "loss": loss, "timing": "host clock around synchronous calls, best of 3"}
+    if peaks is not None:
+        n = sc.fluid.num_particles
+        algo, flops = step_work([sc], xs, ratio)
+        # backward per step: the segment's forward recomputed with its tape written
+        # (310 B per particle), then the adjoint integrate / force / density passes,
+        # which read the tape and the same records as their forward passes
+        bw_algo = 2 * algo + 2 * 310 * n
+        out["roofline_forward"] = pass_roofline("rollout_forward", 1e3 * f / steps, algo, flops,
+                                                *peaks, "c3")
+        out["roofline_backward"] = pass_roofline("rollout_backward", 1e3 * b / steps, bw_algo,
+                                                 3 * flops, *peaks, "c3")
+        out["roofline_backward"]["note"] = ("per step, estimated: recompute (one forward step + "
+                                            "310 B/particle of tape) + adjoint passes (one more "
+                                            "step's bytes + the tape read; twice the forward flops)")
+    return out
 
 
 def measure_batched_adjoint(num: int = 64, steps: int = 100, every: int = 20, reps: int = 2):
@@ -335,17 +497,23 @@ def measure_batched_adjoint(num: int = 64, steps: int = 100, every: int = 20, re
                       "backward one scene after another"}
 
 
-def measure_two_scale(steps: int = 300, warmup: int = 20):
+def measure_two_scale(steps: int = 300, warmup: int = 20, peaks=None):
     """Two-scale dam break (262,144 coarse particles at s = 1/128, refinement slab
     0.35 < x < 0.65, blend increment 0.0125 per step, dt = 2.5e-5): wall time per
-    step of sph2_advance (synchronous: populations are read back every step) and
-    particle-steps/s over both populations, with the split / merge activity seen."""
+    step of sph2_advance (synchronous: populations are read back every step, as
+    the reference reads its counts) and particle-steps/s over both populations,
+    with the split / merge activity seen.  The reference's own two-scale kernels
+    (SPH2S_FINAL_TWO_SCALE/Solver.cu, oracle/ref_harness_ts.cu) are timed from the
+    same state, the populations at the start of the timed window."""
+    from oracle import ref_build
     from sph2s_final_gb300 import scenes
-    from sph2s_final_gb300.two_scale import Solver2
+    from sph2s_final_gb300.two_scale import HIGH, LOW, Solver2
 
     sc = scenes.two_scale_dam_break(1 / 128)
     with Solver2(sc.low, None, sc.boundary, sc.config) as s:
         s.advance(sc.dt, warmup)
+        start = [s.state(LOW), s.state(HIGH)]
+        dbg = [s.debug_step_fields(LOW), s.debug_step_fields(HIGH)]
         part_steps, splits, merges = 0, 0, 0
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -357,18 +525,70 @@ def measure_two_scale(steps: int = 300, warmup: int = 20):
             merges += st["merges"]
         el = time.perf_counter() - t0
         c = s.counts()
-    return {"workload": "two-scale dam break, 262,144 coarse + fine children, slab 0.35<x<0.65, "
-                        "dt 2.5e-5", "steps": steps, "warmup": warmup,
-            "ms_per_step": 1e3 * el / steps, "particle_steps_per_s": part_steps / el,
-            "final_low": c["low"], "final_high": c["high"], "splits": splits, "merges": merges,
-            "timing": "host clock around synchronous sph2_advance calls"}
+    ms = 1e3 * el / steps
+    out = {"workload": "two-scale dam break, 262,144 coarse + fine children, slab 0.35<x<0.65, "
+                       "dt 2.5e-5", "steps": steps, "warmup": warmup,
+           "ms_per_step": ms, "particle_steps_per_s": part_steps / el,
+           "start_low": len(start[0]["ids"]), "start_high": len(start[1]["ids"]),
+           "final_low": c["low"], "final_high": c["high"], "splits": splits, "merges": merges,
+           "timing": "host clock around synchronous sph2_advance calls"}
+    if peaks is not None:
+        # whole-step roofline of the step at the start of the timed window
+        peak_gbs, peak_kind, peak_tf, sms, mhz = peaks
+        g = sc.config.grid
+        h = [float(sc.config.effective_radius[0]), float(sc.config.effective_radius[1])]
+        pos = [st["x"] for st in start]
+        cand = 0
+        for r in (LOW, HIGH):
+            if len(pos[r]) == 0:
+                continue
+            cand += int(stencil_candidates(g[r], h[r], pos[r], pos[r]).sum())
+            if len(pos[1 - r]):
+                cand += int(stencil_candidates(g[1 - r], h[0], pos[r], pos[1 - r]).sum())
+        nbr = sum(int(d["nbr_same"].sum() + d["nbr_compl"].sum()) for d in dbg)
+        bnd = sum(int(d["nbr_boundary"].sum()) for d in dbg)
+        nparts = sum(len(p) for p in pos)
+        flops = (FLOPS_DENS_CAND * cand + FLOPS_DENS_NBR * nbr + FLOPS_FORCE_NBR * nbr
+                 + FLOPS_FORCE_BND * bnd)
+        cells = sum(int(np.prod(list(gg.dims))) for gg in g)
+        # per particle: state in (pos, vel, state, group 40 B), sorted copies out and in
+        # (80 B), keys / values (16 B), density and force records (36 B), next state
+        # out (40 B), compaction (12 B); cell tables 16 B per cell
+        algo = 224 * nparts + 16 * cells
+        out["roofline"] = pass_roofline("two_scale_step", ms, algo, flops, peak_gbs, peak_kind,
+                                        peak_tf, sms, mhz, "c2")
+        out["roofline"]["note"] = ("whole step; bytes 224 per particle + 16 per cell (state in, "
+                                   "sorted copies, keys, records, next state); flops from exact "
+                                   "candidate counts (same and complementary stencils) and the "
+                                   "solver's neighbour counts")
+    try:
+        if not ref_build.CUBIN_TS.exists():
+            raise FileNotFoundError("oracle/_ref/ts_solver.cubin not built")
+        pops = [{"x": st["x"], "v": st["v"], "lam": st["lam"], "state": st["state"]}
+                for st in start]
+        caps = (len(pops[0]["x"]) + 1024, len(pops[1]["x"]) + 8 * len(pops[0]["x"]) + 1024)
+        _, rms, ends = ref_build.run_harness_ts(ref_build.MODE_BLENDED, sc.config, pops,
+                                               sc.boundary.positions, caps, steps, sc.dt,
+                                               warmup=5)
+        n0 = len(pops[0]["x"]) + len(pops[1]["x"])
+        n1 = ends[0] + ends[1]
+        out["reference_gpu"] = {
+            "ms_per_step": rms, "particle_steps_per_s": 0.5 * (n0 + n1) / (rms * 1e-3),
+            "end_low": ends[0], "end_high": ends[1], "speedup_ours": rms / ms,
+            "kind": "reference kernels (SPH2S_FINAL_TWO_SCALE/Solver.cu, unmodified, sm_103a) "
+                    "and its host sequence (thrust sort, per-step count reads) from our state "
+                    "after the warm-up; the reference has no split trigger and no merge, so its "
+                    "populations only fade; CUDA events around whole steps"}
+    except Exception as e:  # reported, not fatal
+        out["reference_gpu"] = {"unavailable": f"{type(e).__name__}: {str(e).splitlines()[0][:200]}"}
+    return out
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    sc, desc = workload(args.workload)
+    sc, desc = workload_reference(args.workload)
     from oracle import oracle as O
     O.set_threads(os.cpu_count() or 1)
     cores = O.num_threads()
@@ -392,7 +612,7 @@ def run_reference(args):
         "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
         "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dam break)",
-        "config": {"workload": desc},
+        "config": config_for(desc, ws),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"FP64 CPU restatement of the reference step (the reference has "
                                    f"no CPU path), {steps} of {args.steps} requested steps"},
@@ -418,8 +638,9 @@ def reference_kernels_on_gpu(sc, args):
     n = sc.fluid.num_particles
     return {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.steps,
             "warmup": max(1, args.warmup),
-            "kind": "reference kernels (Solver.cu, unmodified, sm_103a) + its thrust sort, "
-                    "CUDA events around whole steps"}
+            "kind": "reference kernels (SPH2S_FINAL_SINGLE_SCALE/Solver.cu, unmodified, sm_103a) "
+                    "+ its thrust sort, the same steps and warm-up as our arm, CUDA events "
+                    "around whole steps"}
 
 
 def run_ours(args):
@@ -461,9 +682,17 @@ def run_ours(args):
     clk = clocks.stop()
     value = replicas.throughput(ws * n * args.steps, ms)
 
-    # per-phase kernel durations (CUDA events on the solver's stream)
+    # per-phase kernel durations: the step graph with event nodes between phases
     phases = solver.profile_phases(sc.dt, max(1, min(args.profile_steps, args.steps)))
+    # exact work of the state the phases ended on (debug pass, no advance)
+    dbg = solver.debug_step_fields()
+    xs = solver.positions()
     solver.close()
+    cand = int(stencil_candidates(sc.config.grid, float(sc.config.effective_radius), xs, xs).sum())
+    nbr_self = int(dbg["nbr_fluid"].sum())          # r < h, self included (density)
+    nbr_bnd = int(dbg["nbr_boundary"].sum())
+    work = {"candidates": cand, "fluid_neighbours_with_self": nbr_self,
+            "boundary_neighbours": nbr_bnd}
 
     # end to end through the public API: create from host arrays, then per step
     # advance + positions read back into pinned host memory (sph_get_positions_async:
@@ -490,24 +719,25 @@ def run_ours(args):
         return
 
     peak, peak_kind = measured_peaks()
+    peak_tf, sms, mhz = fp32_peak_tflops(clk.get("sm_mhz"))
     ncells = sc.config.grid.dims[0] * sc.config.grid.dims[1] * sc.config.grid.dims[2]
     btouch = boundary_touched(sc)
+    dens_bytes = 20 * n + 8 * ncells
     force_bytes = 72 * n + 16 * ncells + 16 * btouch
-    dens_bytes = 28 * n + 8 * ncells
-    force_ms, dens_ms = phases["force"], phases["density"]
-    achieved = dens_bytes / (dens_ms * 1e-3) / 1e9
-    f_achieved = force_bytes / (force_ms * 1e-3) / 1e9
+    dens_flops = FLOPS_DENS_CAND * cand + FLOPS_DENS_NBR * nbr_self
+    force_flops = FLOPS_FORCE_NBR * (nbr_self - n) + FLOPS_FORCE_BND * nbr_bnd
+    dens = pass_roofline("density_kernel", phases["density"], dens_bytes, dens_flops, peak,
+                         peak_kind, peak_tf, sms, mhz, args.workload)
+    force = pass_roofline("force_kernel", phases["force"], force_bytes, force_flops, peak,
+                          peak_kind, peak_tf, sms, mhz, args.workload)
     roofline = {"bound": "hbm", "kernel": "density_kernel (the dominant kernel)",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": committed_traffic("density_kernel", args.workload),
-                "algorithmic_bytes_per_launch": dens_bytes,
-                "note": "density and force are FP32-issue / load-latency bound (~216 candidate "
-                        "tests per particle); HBM fraction by compulsory bytes",
-                "force_kernel": {"ms": force_ms, "achieved": f_achieved, "frac": f_achieved / peak,
-                                 "algorithmic_bytes_per_launch": force_bytes,
-                                 "traffic": committed_traffic("force_kernel", args.workload)},
-                "phase_ms": phases}
+                "achieved": dens["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": dens["hbm_frac"], "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": dens["traffic"], "algorithmic_bytes_per_launch": dens_bytes,
+                "density": dens, "force": force, "work": work,
+                "note": "bytes and FP32 fractions per pass; 'binds' names the larger one",
+                "phase_ms": phases,
+                "phase_sum_ms": phases["neighborhood"] + phases["density"] + phases["force"]}
     passes = sort_passes_for(sc.config.grid)
     # kernels per step: from 131,072 particles the step sorts coherently (keys and
     # flags, offsets, compaction, digit offsets, the passes, placement, cell
@@ -519,17 +749,19 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
-        "config": {"workload": desc, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                   "l2": "working set ~0.3 GB > 129 MB L2 (no flush needed)"},
+        "config": config_for(desc, ws),
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
     }
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds)
+        line["cpu_baseline_c0"] = cpu_baseline_c0()
     if ws == 1 and not args.no_extras:
-        line["batched"] = measure_batched(args.batched_steps)
-        line["adjoint"] = measure_adjoint()
+        pk = (peak, peak_kind, peak_tf, sms, mhz)
+        ratio = (nbr_self - n) / max(1, cand)  # neighbours per candidate of the 2M step
+        line["batched"] = measure_batched(args.batched_steps, peaks=pk, ratio=ratio)
+        line["adjoint"] = measure_adjoint(peaks=pk, ratio=ratio)
         line["batched_adjoint"] = measure_batched_adjoint()
-        line["two_scale"] = measure_two_scale()
+        line["two_scale"] = measure_two_scale(peaks=pk)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -186,8 +186,9 @@ int sph_debug_step_fields(sph_solver* s, uint32_t* keys, uint32_t* ids, uint32_t
                           uint32_t* cell_end, uint32_t* nbr_fluid, uint32_t* nbr_boundary,
                           float* rho, float* acc);
 
-/* Advances `steps` steps outside the step graph, timing each phase with CUDA
- * events on the handle's stream; ms[0..2] receive the mean milliseconds per
+/* Advances `steps` steps as one CUDA graph with an event record node at every
+ * phase boundary (the phases run back to back as in the step graph, so they
+ * sum to the span of the steps); ms[0..2] receive the mean milliseconds per
  * step of (hash + sort + reorder + cell ranges), density, force + integrate.
  * (The reference only times the whole Advance, SPH2S_FINAL_SINGLE_SCALE/Solver.cu:1084-1095.) */
 int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms);

@@ -14,6 +14,7 @@ _f = C.POINTER(C.c_float)
 _d = C.POINTER(C.c_double)
 _u = C.POINTER(C.c_uint32)
 _i = C.POINTER(C.c_int32)
+_b = C.POINTER(C.c_uint8)
 _ready = False
 
 
@@ -33,6 +34,9 @@ def lib():
         l.or_ts_last_stats.argtypes = [C.c_void_p, _u]
         l.or_ts_get.argtypes = [C.c_void_p, C.c_int, _d, _d, _f, _i, _u, _u]
         l.or_ts_destroy.argtypes = [C.c_void_p]
+        l.or_ts_decide.argtypes = [C.c_void_p, _u, C.POINTER(_f), C.POINTER(_f), C.POINTER(_i),
+                                   C.POINTER(_u), C.c_uint32, _u, C.POINTER(_b), C.POINTER(_i),
+                                   C.POINTER(_f), C.POINTER(_u)]
         _ready = True
     return l
 
@@ -122,3 +126,31 @@ class TSRollout:
             self.close()
         except Exception:
             pass
+
+
+STAT_NAMES = ("splits", "merges", "removed_low", "removed_high", "faded_in_low", "faded_in_high")
+
+
+def decide(config, pops, group_base):
+    """The state-machine decisions of one slab-trigger step from the
+    start-of-step state (or_ts_decide): the six counters and, per population,
+    keep flags and the state bits, blend coefficients and group ids the
+    particles leave the step with.  pops = [low, high] dicts of x (n,3), lam,
+    state, group."""
+    arr = []
+    for p in pops:
+        arr.append({"x": np.ascontiguousarray(p["x"], np.float32).reshape(-1, 3),
+                    "lam": np.ascontiguousarray(p["lam"], np.float32),
+                    "state": np.ascontiguousarray(p["state"], np.int32),
+                    "group": np.ascontiguousarray(p["group"], np.uint32)})
+    n = np.array([a["x"].shape[0] for a in arr], np.uint32)
+    out = [{"keep": np.empty(k, np.uint8), "state": np.empty(k, np.int32),
+            "lam": np.empty(k, np.float32), "group": np.empty(k, np.uint32)} for k in n]
+    stats = np.zeros(6, np.uint32)
+    lib().or_ts_decide(C.byref(config), n.ctypes.data_as(_u),
+                       _pp([a["x"] for a in arr], _f), _pp([a["lam"] for a in arr], _f),
+                       _pp([a["state"] for a in arr], _i), _pp([a["group"] for a in arr], _u),
+                       int(group_base), stats.ctypes.data_as(_u),
+                       _pp([o["keep"] for o in out], _b), _pp([o["state"] for o in out], _i),
+                       _pp([o["lam"] for o in out], _f), _pp([o["group"] for o in out], _u))
+    return dict(zip(STAT_NAMES, map(int, stats))), out

@@ -564,6 +564,74 @@ void or_ts_get(void* h, int r, double* x, double* v, float* lam, int32_t* state,
     if (ids) std::memcpy(ids, p.ids.data(), n * 4);
 }
 
+// The blend / state-machine decisions of one slab-trigger step
+// (SPH2S_FINAL_TWO_SCALE/Solver.cu:1229-1289 plus the slab split and group
+// merge rules of ts_step above) from the start-of-step state alone: they
+// depend on positions only through the slab test of each LOW particle and of
+// each group's fixed-point centroid, never on the step's physics.  stats =
+// splits, merges, removed LOW, removed HIGH, faded-in LOW, faded-in HIGH;
+// per particle (each output optional): keep (survives the step), the state
+// bits, blend coefficient and group id it leaves the step with.  Blended mode
+// with the slab trigger only.
+void or_ts_decide(const OConfig2* C, const uint32_t* n, const float* const* x,
+                  const float* const* lam, const int32_t* const* state,
+                  const uint32_t* const* group, uint32_t group_base, uint32_t* stats,
+                  uint8_t* const* keep, int32_t* const* next_state, float* const* next_lam,
+                  uint32_t* const* next_group) {
+    const bool refine = C->refine_axis >= 0 && C->refine_axis < 3;
+    const int ax = refine ? C->refine_axis : 0;
+    std::vector<int64_t> gsum(group_base, 0);
+    std::vector<uint32_t> gready(group_base, 0);
+    for (uint32_t k = 0; k < n[HIGH]; ++k) {
+        const uint32_t g = group[HIGH][k];
+        if (g == kNoGroup || g >= group_base) continue;
+        gsum[g] += fixed40(x[HIGH][3 * k + ax]);
+        gready[g] += state[HIGH][k] == 4 ? 1u : 0u;
+    }
+    const int64_t L = fixed43(C->refine_lo), H = fixed43(C->refine_hi);
+    std::vector<uint8_t> merge(group_base, 0);
+    uint32_t merges = 0;
+    for (uint32_t g = 0; g < group_base; ++g) {
+        merge[g] = refine && gready[g] == 8 && !(L < gsum[g] && gsum[g] < H);
+        merges += merge[g];
+    }
+    const float cblend[4] = {0.0f, -1.0f, 1.0f, 0.0f};
+    uint32_t st[6] = {0, merges, 0, 0, 0, 0};
+    for (int r = HIGH; r >= LOW; --r)
+        for (uint32_t i = 0; i < n[r]; ++i) {
+            int32_t s = state[r][i];
+            uint32_t g = group[r][i];
+            const float xa = x[r][3 * i + ax];
+            if (r == LOW && refine && (s & 3) == 0 && C->refine_lo < xa && xa < C->refine_hi)
+                s = (s & 4) | 3;
+            float l = lam[r][i] + cblend[s & 3] * C->blend_increment;
+            uint8_t kp = 1;
+            if (l <= 0.0f && (s & 3) == 1) {
+                st[2 + r]++;
+                kp = 0;
+            } else {
+                if (l >= 1.0f && (s & 3) == 2) {
+                    s &= 4;
+                    l = 1.0f;
+                    st[4 + r]++;
+                }
+                if (r == LOW && (s & 3) == 3) {
+                    st[0]++;
+                    s = 1;
+                }
+                if (r == HIGH && g != kNoGroup && g < group_base && merge[g]) {
+                    s = 5;
+                    g = kNoGroup;
+                }
+            }
+            if (keep && keep[r]) keep[r][i] = kp;
+            if (next_state && next_state[r]) next_state[r][i] = s;
+            if (next_lam && next_lam[r]) next_lam[r][i] = l;
+            if (next_group && next_group[r]) next_group[r][i] = g;
+        }
+    for (int k = 0; k < 6; ++k) stats[k] = st[k];
+}
+
 void or_ts_destroy(void* h) { delete (TSState*)h; }
 
 }  // extern "C"

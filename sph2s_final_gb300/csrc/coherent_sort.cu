@@ -311,7 +311,11 @@ __global__ void __launch_bounds__(256) coherent_cells_kernel(const uint32_t* __r
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t key = keys[i];
-    kprev[i] = key;
+    // After a look-back timeout earlier in this sort (err bit 1, set only by
+    // previous kernels, so every thread sees the same value) the keys are not
+    // sorted; 0xFFFFFFFF everywhere keeps kprev non-decreasing and makes every
+    // particle a mover in the next step, which then sorts from scratch.
+    kprev[i] = (*(volatile const uint32_t*)err & 1u) ? 0xFFFFFFFFu : key;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
     const uint32_t c = morton_to_linear_checked(g, key);
     if (c == kEmptyCell) {

@@ -543,29 +543,50 @@ int sph_profile_phases(sph_solver* s, float dt, int32_t steps, float* ms) {
     if (!s || !ms || steps < 0) return fail(SPH_E_INVALID, "sph_profile_phases: bad argument");
     ms[0] = ms[1] = ms[2] = 0.0f;
     if (s->n == 0 || steps == 0) return SPH_OK;
-    cudaEvent_t ev[4];
-    for (auto& e : ev) SPH_CUDA(cudaEventCreate(&e));
-    float acc[3] = {0, 0, 0};
+    // The steps are captured into one graph with an event record node at each
+    // phase boundary, so the phases are timed as the step graph runs them
+    // (back to back, no host launches in between); they sum to the whole span.
+    std::vector<cudaEvent_t> ev(3 * (size_t)steps + 1, nullptr);
     cudaError_t err = cudaSuccess;
-    for (int k = 0; k < steps && err == cudaSuccess; ++k) {
-        cudaEventRecord(ev[0], s->stream);
-        enqueue_neighborhood(s);
-        cudaEventRecord(ev[1], s->stream);
-        enqueue_density(s);
-        cudaEventRecord(ev[2], s->stream);
-        enqueue_force(s, dt);
-        cudaEventRecord(ev[3], s->stream);
-        err = cudaGetLastError();
-        if (err == cudaSuccess) err = cudaEventSynchronize(ev[3]);
+    for (auto& e : ev)
+        if (err == cudaSuccess) err = cudaEventCreate(&e);
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    if (err == cudaSuccess) err = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) {
+        // cudaEventRecordExternal: a real event record node (a plain record
+        // during capture only orders streams)
+        const unsigned fl = cudaEventRecordExternal;
+        for (int k = 0; k < steps; ++k) {
+            if (k == 0) cudaEventRecordWithFlags(ev[0], s->stream, fl);
+            enqueue_neighborhood(s);
+            cudaEventRecordWithFlags(ev[3 * k + 1], s->stream, fl);
+            enqueue_density(s);
+            cudaEventRecordWithFlags(ev[3 * k + 2], s->stream, fl);
+            enqueue_force(s, dt);
+            cudaEventRecordWithFlags(ev[3 * k + 3], s->stream, fl);
+        }
+        cudaError_t le = cudaGetLastError();
+        err = cudaStreamEndCapture(s->stream, &g);
+        if (err == cudaSuccess) err = le;
+    }
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&ge, g, 0);
+    if (err == cudaSuccess) err = cudaGraphLaunch(ge, s->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+    double acc[3] = {0, 0, 0};
+    for (int k = 0; k < steps && err == cudaSuccess; ++k)
         for (int p = 0; p < 3 && err == cudaSuccess; ++p) {
             float t = 0.0f;
-            err = cudaEventElapsedTime(&t, ev[p], ev[p + 1]);
+            err = cudaEventElapsedTime(&t, ev[3 * k + p], ev[3 * k + p + 1]);
             acc[p] += t;
         }
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
     SPH_CUDA(err);
-    for (int p = 0; p < 3; ++p) ms[p] = acc[p] / (float)steps;
+    s->step += (uint64_t)steps;
+    for (int p = 0; p < 3; ++p) ms[p] = (float)(acc[p] / steps);
     return check_device_error(s);
 }
 

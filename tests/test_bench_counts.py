@@ -1,0 +1,36 @@
+"""bench.py's work counts for the roofline: stencil candidates by summed-area
+table equal a direct count over the same stencil rule (the oracle's stencil),
+including particles outside the grid (clamped cells)."""
+import numpy as np
+
+import bench
+from oracle import oracle as O
+from sph2s_final_gb300 import scenes
+
+
+def test_stencil_candidates_match_direct_count():
+    sc = scenes.dam_break(1 / 16)
+    x = sc.fluid.positions.copy()
+    rng = np.random.default_rng(4)
+    x[:20] = rng.uniform(-0.1, 1.1, (20, 3)).astype(np.float32)  # some outside the grid
+    g = sc.config.grid
+    h = float(sc.config.effective_radius)
+    got = bench.stencil_candidates(g, h, x, x)
+    cs, ce = O.stencil(g, x, h)
+    _, lin = O.cell_keys(g, x)
+    d = np.array(g.dims[:])
+    cz, rem = np.divmod(lin.astype(np.int64), d[0] * d[1])
+    cy, cx = np.divmod(rem, d[0])
+    want = np.array([np.sum((cx >= cs[i, 0]) & (cx <= ce[i, 0]) & (cy >= cs[i, 1]) & (cy <= ce[i, 1])
+                            & (cz >= cs[i, 2]) & (cz <= ce[i, 2])) for i in range(len(x))])
+    np.testing.assert_array_equal(got, want)
+
+
+def test_reference_workload_loads_no_product_code():
+    import subprocess
+    import sys
+    code = ("import sys, bench; sc, d = bench.workload_reference('c0'); "
+            "assert not any(m.startswith('sph2s_final_gb300') for m in sys.modules), "
+            "sorted(m for m in sys.modules if m.startswith('sph2s'))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
