@@ -57,7 +57,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=100)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c0"], default="c1")
+    ap.add_argument("--workload", choices=["c1", "c0", "c1m"], default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile-steps", type=int, default=200)
@@ -70,6 +70,9 @@ WORKLOADS = {
     "c1": (1 / 256, "dam break 2,097,152 fluid + 2,043,880 boundary, s=1/256, h=2s, 128^3 cells, "
                     "dt=2.5e-5"),
     "c0": (1 / 64, "dam break 32,768 fluid + 143,080 boundary, s=1/64, h=2s, 32^3 cells, dt=1e-4"),
+    # a mid-size case for one-kernel ncu captures: above the 129 MB L2, far below the 2M case
+    "c1m": (1 / 160, "dam break 512,000 fluid + 817,000 boundary, s=1/160, h=2s, 80^3 cells, "
+                     "dt=2.5e-5"),
 }
 
 

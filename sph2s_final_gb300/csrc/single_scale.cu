@@ -149,9 +149,8 @@ int check_device_error(sph_solver* s) {
     return SPH_OK;
 }
 
-int create_solver(const sph_config* config, const float4* hpos, const float4* hvel,
-                  const float4* hpos0, uint32_t n_fluid, const float4* hbound, uint32_t n_boundary,
-                  uint64_t step, sph_solver** out) {
+int create_solver(const sph_config* config, const HostInit& init, uint32_t n_fluid,
+                  uint32_t n_boundary, uint64_t step, sph_solver** out) {
     *out = nullptr;
     SimParams P;
     int rc = make_sim_params(*config, &P);
@@ -209,19 +208,51 @@ int create_solver(const sph_config* config, const float4* hpos, const float4* hv
     }
     TRY(check_cuda(cudaMemsetAsync(s->rho, 0, 4 * (size_t)(n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
 
-    // Upload the fluid state (float4, persistent id in w).
+    // Upload the fluid state (float4, persistent id in w).  Raw caller xyz
+    // arrays go up as they are (12 bytes per particle) into the step buffers,
+    // which are free until the first step, and are packed on the device.
     {
-        if (n_fluid) {
-            TRY(check_cuda(cudaMemcpyAsync(s->pos, hpos, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
-            TRY(check_cuda(cudaMemcpyAsync(s->vel, hvel, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
-            TRY(check_cuda(cudaMemcpyAsync(s->pos0, hpos0, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+        if (n_fluid && init.pos_xyz) {
+            const size_t bytes = 12 * (size_t)n_fluid;
+            TRY(check_cuda(cudaMemcpyAsync(s->spos, init.pos_xyz, bytes, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            unpack_xyz_kernel<<<blocks_for(n_fluid), 256, 0, s->stream>>>(
+                reinterpret_cast<const float*>(s->spos), n_fluid, 1, s->pos);
+            if (init.vel_xyz) {
+                TRY(check_cuda(cudaMemcpyAsync(s->svel, init.vel_xyz, bytes, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+                unpack_xyz_kernel<<<blocks_for(n_fluid), 256, 0, s->stream>>>(
+                    reinterpret_cast<const float*>(s->svel), n_fluid, 0, s->vel);
+            } else {
+                TRY(check_cuda(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n_fluid, s->stream), "memset", __FILE__, __LINE__));
+            }
+            TRY(check_cuda(cudaMemcpyAsync(s->pos0, s->pos, sizeof(float4) * n_fluid, cudaMemcpyDeviceToDevice, s->stream), "copy", __FILE__, __LINE__));
+            TRY(check_cuda(cudaGetLastError(), "unpack", __FILE__, __LINE__));
+        } else if (n_fluid) {
+            TRY(check_cuda(cudaMemcpyAsync(s->pos, init.pos, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->vel, init.vel, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
+            TRY(check_cuda(cudaMemcpyAsync(s->pos0, init.pos0, sizeof(float4) * n_fluid, cudaMemcpyHostToDevice, s->stream), "upload", __FILE__, __LINE__));
         }
         // Boundary: hashed and sorted once on the fluid grid (Solver.cu:1013-1055).
         TRY(check_cuda(cudaMemsetAsync(s->bcells, 0xFF, sizeof(uint2) * s->ncells, s->stream), "memset", __FILE__, __LINE__));
         if (n_boundary) {
-            float4* braw = nullptr;
-            TRY(dalloc(&braw, n_boundary));
-            cudaError_t e = cudaMemcpyAsync(braw, hbound, sizeof(float4) * n_boundary, cudaMemcpyHostToDevice, s->stream);
+            // the unsorted boundary in float4 (input index in w): in the force
+            // records' buffer when it is large enough (unused until the first
+            // density pass), else a temporary allocation
+            float4* braw = s->xa;
+            const bool own = n_boundary > n_fluid;
+            if (own) TRY(dalloc(&braw, n_boundary));
+            cudaError_t e;
+            if (init.bound_xyz) {  // raw xyz staged in bpos (overwritten by the presort)
+                e = cudaMemcpyAsync(s->bpos, init.bound_xyz, 12 * (size_t)n_boundary,
+                                    cudaMemcpyHostToDevice, s->stream);
+                if (e == cudaSuccess) {
+                    unpack_xyz_kernel<<<blocks_for(n_boundary), 256, 0, s->stream>>>(
+                        reinterpret_cast<const float*>(s->bpos), n_boundary, 1, braw);
+                    e = cudaGetLastError();
+                }
+            } else {
+                e = cudaMemcpyAsync(braw, init.bound, sizeof(float4) * n_boundary,
+                                    cudaMemcpyHostToDevice, s->stream);
+            }
             if (e == cudaSuccess) {
                 // keys (cell, depth class): each cell's boundary particles by
                 // non-decreasing depth, the order boundary_reach's cut needs
@@ -239,7 +270,7 @@ int create_solver(const sph_config* config, const float4* hpos, const float4* hv
                 e = cudaGetLastError();
                 if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
             }
-            cudaFree(braw);
+            if (own) cudaFree(braw);
             TRY(check_cuda(e, "boundary presort", __FILE__, __LINE__));
         }
         const int reach = (int)std::ceil(config->effective_radius / config->grid.spacing) + 1;
@@ -285,23 +316,11 @@ int sph_create(const sph_config* config, const float* fluid_xyz, uint32_t n_flui
     if (n_boundary && !boundary_xyz) return fail(SPH_E_INVALID, "sph_create: NULL boundary positions");
     if (n_fluid > kMaxParticles || n_boundary > kMaxParticles)
         return fail(SPH_E_CAPACITY, "sph_create: more than 2^30 particles");
-    // float4 with the persistent id (fluid) / input index (boundary) in w
-    std::vector<float4> hp(n_fluid), hv(n_fluid), hb(n_boundary);
-    for (uint32_t i = 0; i < n_fluid; ++i) {
-        float w;
-        std::memcpy(&w, &i, 4);
-        hp[i] = make_float4(fluid_xyz[3 * i], fluid_xyz[3 * i + 1], fluid_xyz[3 * i + 2], w);
-        hv[i] = velocity_xyz ? make_float4(velocity_xyz[3 * i], velocity_xyz[3 * i + 1],
-                                           velocity_xyz[3 * i + 2], 0.0f)
-                             : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    for (uint32_t i = 0; i < n_boundary; ++i) {
-        float w;
-        std::memcpy(&w, &i, 4);
-        hb[i] = make_float4(boundary_xyz[3 * i], boundary_xyz[3 * i + 1], boundary_xyz[3 * i + 2], w);
-    }
-    return sph_ss::create_solver(config, hp.data(), hv.data(), hp.data(), n_fluid, hb.data(),
-                                 n_boundary, 0, out);
+    sph_ss::HostInit init;
+    init.pos_xyz = fluid_xyz;
+    init.vel_xyz = velocity_xyz;
+    init.bound_xyz = boundary_xyz;
+    return sph_ss::create_solver(config, init, n_fluid, n_boundary, 0, out);
 }
 
 int sph_advance(sph_solver* s, float dt, int32_t steps) {

@@ -120,6 +120,17 @@ static __global__ void __launch_bounds__(256) pack_xyz_kernel(const float4* __re
     dst[3 * (size_t)d + 2] = v.z;
 }
 
+// Caller xyz (3 floats per particle) -> float4; w = the input index as bits
+// (a persistent id) or 0.
+static __global__ void __launch_bounds__(256) unpack_xyz_kernel(const float* __restrict__ xyz,
+                                                         uint32_t n, int with_id,
+                                                         float4* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const size_t b = 3 * (size_t)k;
+    out[k] = make_float4(xyz[b], xyz[b + 1], xyz[b + 2], with_id ? __uint_as_float(k) : 0.0f);
+}
+
 // Scalar field (one float per particle) into a caller's array, in sorted order
 // or scattered by the persistent ids in ids[k].w.
 static __global__ void __launch_bounds__(256) pack_scalar_kernel(const float* __restrict__ src,

@@ -72,12 +72,19 @@ int check_device_error(sph_solver* s);
 // Selects the integrator (allocating the XSPH buffers on first use) and drops
 // the captured step graph.
 int set_integrator(sph_solver* s, int32_t integrator);
-// Creates a handle from host float4 arrays: fluid positions (persistent id in
-// w) and velocities in the order the next step starts from, creation-time
-// positions (rollout restarts), boundary positions (presorted here).
-int create_solver(const sph_config* config, const float4* hpos, const float4* hvel,
-                  const float4* hpos0, uint32_t n_fluid, const float4* hbound, uint32_t n_boundary,
-                  uint64_t step, sph_solver** out);
+// Host arrays a handle is created from: either packed float4 arrays (a saved
+// state: fluid positions with the persistent id in w and velocities in the
+// order the next step starts from, creation-time positions for rollout
+// restarts, boundary positions) or the caller's raw xyz arrays (sph_create:
+// 3 floats per particle, ids = input order, velocities NULL = zero), which are
+// copied as they are and packed into float4 on the device.
+struct HostInit {
+    const float4 *pos = nullptr, *vel = nullptr, *pos0 = nullptr, *bound = nullptr;
+    const float *pos_xyz = nullptr, *vel_xyz = nullptr, *bound_xyz = nullptr;
+};
+// Creates a handle (boundary presorted here).
+int create_solver(const sph_config* config, const HostInit& init, uint32_t n_fluid,
+                  uint32_t n_boundary, uint64_t step, sph_solver** out);
 inline uint32_t blocks_for(uint32_t n, uint32_t t = 256) { return (n + t - 1) / t; }
 }  // namespace sph_ss
 

@@ -107,8 +107,12 @@ int sph_create_from_state(const void* src, uint64_t bytes, sph_solver** out) {
     r.get(bpos.data(), 16 * (size_t)nb);
     if (!ids_are_permutation(pos))
         return fail(SPH_E_INVALID, "sph_create_from_state: persistent ids are not a permutation");
-    int rc = sph_ss::create_solver(&cfg, pos.data(), vel.data(), pos0.data(), n, bpos.data(), nb,
-                                   pre.step, out);
+    sph_ss::HostInit init;
+    init.pos = pos.data();
+    init.vel = vel.data();
+    init.pos0 = pos0.data();
+    init.bound = bpos.data();
+    int rc = sph_ss::create_solver(&cfg, init, n, nb, pre.step, out);
     if (rc == SPH_OK && integrator != SPH_INTEGRATOR_SYMPLECTIC_EULER) {
         rc = sph_ss::set_integrator(*out, integrator);
         if (rc != SPH_OK) {
