@@ -52,9 +52,10 @@ __device__ __forceinline__ void force_one(
     ForceAcc A = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const uint32_t kc = nbr_count[i];
     if (kc <= (uint32_t)kMaxNbr) {
-        uint4 g = kc ? __ldg(&nbr4[i]) : make_uint4(0u, 0u, 0u, 0u);
+        // list groups are read once: streaming loads (evict-first)
+        uint4 g = kc ? __ldcs(&nbr4[i]) : make_uint4(0u, 0u, 0u, 0u);
         for (uint32_t t = 0; t < kc; t += 4) {
-            const uint4 gn = (t + 4 < kc) ? __ldg(&nbr4[(size_t)((t >> 2) + 1) * n + i]) : g;
+            const uint4 gn = (t + 4 < kc) ? __ldcs(&nbr4[(size_t)((t >> 2) + 1) * n + i]) : g;
             const uint32_t js[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
             for (int u = 0; u < 4; ++u) {

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                             s = fmaf(P.coupled ? 1.0f : xj.w, a * a * a, s);
                             if (DEBUG) ++ns;
                             if (r2 != 0.0f) {
-                                if (k < (uint32_t)kMaxNbr) *out = j;
+                                if (k < (uint32_t)kMaxNbr) __stcs(out, j);  // lists: evict-first
                                 out += (k & 3u) == 3u ? next_group : 1u;
                                 ++k;
                             }
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) ts_density_kernel(
                             sc = fmaf(P.coupled ? 1.0f : xj.w, 0.5f * w, sc);
                             if (DEBUG) ++nc;
                             if (r2 != 0.0f) {
-                                if (kcl < ComplCap<R>::value) *cout = j;
+                                if (kcl < ComplCap<R>::value) __stcs(cout, j);
                                 cout += (kcl & 3u) == 3u ? next_group : 1u;
                                 ++kcl;
                             }
@@ -340,9 +340,9 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         };
         const uint32_t kc = list_count[i];
         if (kc <= (uint32_t)kMaxNbr) {  // the density pass's list, in stencil order
-            uint4 g = kc ? __ldg(&list4[i]) : make_uint4(0u, 0u, 0u, 0u);
+            uint4 g = kc ? __ldcs(&list4[i]) : make_uint4(0u, 0u, 0u, 0u);
             for (uint32_t t = 0; t < kc; t += 4) {
-                const uint4 gn = (t + 4 < kc) ? __ldg(&list4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
+                const uint4 gn = (t + 4 < kc) ? __ldcs(&list4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
                 const uint32_t js[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
@@ -410,10 +410,10 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
         };
         const uint32_t kc = clist_count[i];
         if (kc <= ComplCap<R>::value) {  // the density pass's list, in stencil order
-            uint4 gc = kc ? __ldg(&clist4[i]) : make_uint4(0u, 0u, 0u, 0u);
+            uint4 gc = kc ? __ldcs(&clist4[i]) : make_uint4(0u, 0u, 0u, 0u);
             for (uint32_t t = 0; t < kc; t += 4) {
                 const uint4 g = gc;  // this group; the next one is fetched meanwhile
-                gc = (t + 4 < kc) ? __ldg(&clist4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
+                gc = (t + 4 < kc) ? __ldcs(&clist4[(size_t)((t >> 2) + 1) * n_r + i]) : g;
                 const uint32_t js[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
