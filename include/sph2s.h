@@ -317,6 +317,12 @@ int sph2_get_state(sph_solver2* s, int32_t population, float* xyz, float* vel, f
  * ParticleData::dPositions (SPH2S_FINAL_TWO_SCALE/ParticleData.h:38-43).
  * Asynchronous; a destination that is not device memory: SPH_E_INVALID. */
 int sph2_get_positions_device(sph_solver2* s, int32_t population, float* d_xyz);
+/* State bits of one population in its current order (one int32 per
+ * particle) copied into caller-owned device memory on the handle's stream:
+ * the two-scale ParticleData::dStates the reference's renderer reads
+ * (SPH2S_FINAL_TWO_SCALE/ParticleData.h:43).  Asynchronous; a destination
+ * that is not device memory: SPH_E_INVALID. */
+int sph2_get_states_device(sph_solver2* s, int32_t population, int32_t* d_state);
 /* Parity instrumentation: for the current state, without advancing, the
  * sorted persistent ids, densities, accelerations and neighbour counts (same
  * population, complementary population, boundary) of one population, in the

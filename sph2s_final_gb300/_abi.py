@@ -107,6 +107,7 @@ SIGNATURES = {
     "sph_get_velocities_device": (C.c_int, [_vp, C.c_void_p, C.c_int32]),
     "sph_get_densities_device": (C.c_int, [_vp, C.c_void_p, C.c_int32]),
     "sph2_get_positions_device": (C.c_int, [_vp, C.c_int32, C.c_void_p]),
+    "sph2_get_states_device": (C.c_int, [_vp, C.c_int32, C.c_void_p]),
     "sph_get_ids": (C.c_int, [_vp, _u]),
     "sph_set_velocities": (C.c_int, [_vp, _f, C.c_int32]),
     "sph_counts": (C.c_int, [_vp, _u, _u]),

@@ -641,6 +641,18 @@ int sph2_get_positions_device(sph_solver2* s, int32_t population, float* d_xyz) 
     return SPH_OK;
 }
 
+int sph2_get_states_device(sph_solver2* s, int32_t population, int32_t* d_state) {
+    if (!s || population < 0 || population > 1)
+        return fail(SPH_E_INVALID, "sph2_get_states_device: bad handle or population");
+    Pop& p = s->pop[population];
+    if (p.n == 0) return SPH_OK;
+    if (!d_state) return fail(SPH_E_INVALID, "sph2_get_states_device: NULL destination");
+    int rc = sph::check_device_pointer(d_state, "sph2_get_states_device");
+    if (rc != SPH_OK) return rc;
+    SPH_CUDA(cudaMemcpyAsync(d_state, p.stt, 4 * (size_t)p.n, cudaMemcpyDeviceToDevice, s->stream));
+    return SPH_OK;
+}
+
 int sph2_debug_step_fields(sph_solver2* s, int32_t population, uint32_t* ids_sorted, float* rho,
                            float* acc, uint32_t* nbr_same, uint32_t* nbr_compl,
                            uint32_t* nbr_boundary) {

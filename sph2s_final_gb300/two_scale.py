@@ -108,6 +108,11 @@ class Solver2:
         per particle) into caller-owned device memory on the solver's stream."""
         check(lib().sph2_get_positions_device(self._h, population, C.c_void_p(device_ptr)))
 
+    def read_states_device(self, population: int, device_ptr: int) -> None:
+        """Enqueues a copy of one population's state bits (int32, current order)
+        into caller-owned device memory on the solver's stream."""
+        check(lib().sph2_get_states_device(self._h, population, C.c_void_p(device_ptr)))
+
     def debug_step_fields(self, population: int) -> dict:
         n = self.counts()["low" if population == LOW else "high"]
         r = {"ids": np.empty(n, np.uint32), "rho": np.empty(n, np.float32),

@@ -4,7 +4,10 @@ classes that forward to include/sph2s.h), each driving a scene built with the
 ABI's grid, particle-box and configuration builders; tests/cabi_client3.cpp is
 the reference's own host-program flow (initSim / display) on the header-only
 drop-in include/sph2s_solver.hpp (Grid, SolverConfiguration, ParticleData with
-device arrays, Solver(ParticleData*, ParticleData*, const SolverConfiguration*)).
+device arrays, Solver(ParticleData*, ParticleData*, const SolverConfiguration*)),
+and tests/cabi_client4.cpp the two-scale program's flow on
+include/sph2s_solver2.hpp (Solver(low, high, boundary, config), ParticleData
+with dPositions, dStates and NumParticles kept current by every Advance).
 
 CPU: the header compiles as C99 and as C++17 with warnings as errors, and both
 clients link against libsph2s.so.  GPU: each client's run equals the same run
@@ -42,7 +45,7 @@ def build_client(tmp_path, name="cabi_client"):
     cmd = [compiler("g++"), "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
            "-I", str(ROOT / "include"), str(ROOT / "tests" / f"{name}.cpp"),
            "-L", str(PKG), "-lsph2s", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
-    if name == "cabi_client3":  # the drop-in header allocates ParticleData with the CUDA runtime
+    if name in ("cabi_client3", "cabi_client4"):  # the drop-in headers allocate with the CUDA runtime
         if not (CUDA_HOME / "include" / "cuda_runtime.h").exists():
             pytest.skip("CUDA runtime headers not found")
         cmd[-2:-2] = ["-isystem", str(CUDA_HOME / "include"), "-L", str(CUDA_HOME / "lib64"),
@@ -61,7 +64,7 @@ def test_header_compiles_as_c(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.parametrize("name", ["cabi_client", "cabi_client2", "cabi_client3"])
+@pytest.mark.parametrize("name", ["cabi_client", "cabi_client2", "cabi_client3", "cabi_client4"])
 def test_client_compiles_and_links(tmp_path, name):
     assert build_client(tmp_path, name).exists()
 
@@ -185,3 +188,49 @@ def test_reference_host_flow_on_the_drop_in_header(tmp_path):
         np.testing.assert_array_equal(s.ids(), ids)
         np.testing.assert_array_equal(s.positions("sorted"), x)
     assert np.abs(x[np.argsort(ids)] - fluid).max() > 0  # the client did step the scene
+
+
+def read_run4(path):
+    data = path.read_bytes()
+    nl, nb, steps = struct.unpack_from("<III", data, 0)
+    (dt,) = struct.unpack_from("<f", data, 12)
+    off = 16
+    cfg = _abi.sph_config2.from_buffer_copy(data, off)
+    off += C.sizeof(_abi.sph_config2)
+
+    def take(dtype, count):
+        nonlocal off
+        a = np.frombuffer(data, dtype, count, off).copy()
+        off += 4 * count
+        return a
+
+    low = take(np.float32, 3 * nl).reshape(nl, 3)
+    boundary = take(np.float32, 3 * nb).reshape(nb, 3)
+    pops = []
+    for _ in (LOW, HIGH):
+        (n,) = struct.unpack_from("<I", data, off)
+        off += 4
+        pops.append({"x": take(np.float32, 3 * n).reshape(n, 3), "state": take(np.int32, n),
+                     "ids": take(np.uint32, n)})
+    assert off == len(data)
+    return cfg, low, boundary, steps, dt, pops
+
+
+@pytest.mark.gpu
+def test_two_scale_reference_host_flow_on_the_drop_in_header(tmp_path):
+    """The two-scale initSim / display through include/sph2s_solver2.hpp: after
+    every Advance both ParticleData hold the solver's positions, state bits and
+    counts; after 25 steps they equal the Python binding's, bit for bit."""
+    exe = build_client(tmp_path, "cabi_client4")
+    out = tmp_path / "run4.bin"
+    r = subprocess.run([str(exe), str(out), "25"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cfg, low, boundary, steps, dt, pops = read_run4(out)
+    assert steps == 25 and low.shape[0] > 10000 and cfg.refine_axis == 0
+    assert pops[HIGH]["ids"].size > 0  # the slab refined part of the block
+    with Solver2(low, None, boundary, cfg, low.shape[0], 8 * low.shape[0]) as s:
+        s.advance(dt, steps)
+        for pop in (LOW, HIGH):
+            st = s.state(pop)
+            for k in ("ids", "x", "state"):
+                np.testing.assert_array_equal(pops[pop][k], st[k], err_msg=f"{pop} {k}")

@@ -36,7 +36,8 @@ def test_async_readback_matches_sync_readback():
 def test_device_readback_matches_host_readback():
     """sph_get_positions/_velocities/_densities_device write the host readback's
     arrays into caller-owned device memory, in both orders; sph2's positions
-    likewise; a host destination is refused before any kernel runs."""
+    and state bits likewise; a host destination is refused before any kernel
+    runs."""
     from sph2s_final_gb300 import _abi
     from sph2s_final_gb300.two_scale import HIGH, LOW, Solver2
     sc = scenes.dam_break(1 / 32)
@@ -66,3 +67,8 @@ def test_device_readback_matches_host_readback():
             s2.read_positions_device(pop, d.data_ptr())
             torch.cuda.synchronize()
             np.testing.assert_array_equal(d.cpu().numpy(), w)
+            ws = s2.state(pop)["state"]
+            ds = torch.empty(ws.shape, dtype=torch.int32, device="cuda")
+            s2.read_states_device(pop, ds.data_ptr())
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(ds.cpu().numpy(), ws)
