@@ -102,10 +102,35 @@ def workload_reference(name: str):
     return sc, desc
 
 
-def config_for(desc: str, ws: int) -> dict:
-    """The `config` object of both arms' lines."""
+# Device bytes a step touches per fluid particle (state and step copies 64, density /
+# aux 12, force records 16, neighbour lists ~136 used, keys and sort scratch ~24, the
+# coherent sort's flags and previous keys ~8), per cell (fluid and boundary tables,
+# 16) and per boundary particle (16).
+STEP_BYTES_PER_PARTICLE, STEP_BYTES_PER_CELL, STEP_BYTES_PER_BOUNDARY = 260, 16, 16
+
+
+def l2_bytes() -> tuple[int, str]:
+    """The GPU's L2 size (cudaDevAttrL2CacheSize through torch), else the GB300's 129 MB."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return int(torch.cuda.get_device_properties(0).L2_cache_size), "queried"
+    except Exception:
+        pass
+    return 129 * 2**20, "nominal"
+
+
+def config_for(desc: str, ws: int, sc) -> dict:
+    """The `config` object of both arms' lines: the workload and whether its per-step
+    data exceeds L2 (then no flush is needed between timed steps)."""
+    g = sc.config.grid
+    cells = int(g.dims[0]) * int(g.dims[1]) * int(g.dims[2])
+    ws_bytes = (STEP_BYTES_PER_PARTICLE * sc.fluid.num_particles + STEP_BYTES_PER_CELL * cells
+                + STEP_BYTES_PER_BOUNDARY * sc.boundary.num_particles)
+    l2, how = l2_bytes()
+    rel = "> L2, no flush needed" if ws_bytes > l2 else "fits in L2 (a parity-size case, not flushed)"
     return {"workload": desc, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-            "l2": "working set ~0.3 GB > 129 MB L2 (no flush needed)"}
+            "l2": f"per-step data ~{ws_bytes / 2**20:.0f} MiB, L2 {l2 / 2**20:.0f} MiB ({how}): {rel}"}
 
 
 def dist_env():
@@ -621,7 +646,7 @@ def run_reference(args):
         "steps": steps, "steps_requested": args.steps, "warmup": warm + 1,
         "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dam break)",
-        "config": config_for(desc, ws),
+        "config": config_for(desc, ws, sc),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"FP64 CPU restatement of the reference step (the reference has "
                                    f"no CPU path), {steps} of {args.steps} requested steps"},
@@ -760,7 +785,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
-        "config": config_for(desc, ws),
+        "config": config_for(desc, ws, sc),
         "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
     }
     if ws == 1 and not args.no_cpu_baseline:

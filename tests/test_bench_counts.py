@@ -34,3 +34,15 @@ def test_reference_workload_loads_no_product_code():
             "sorted(m for m in sys.modules if m.startswith('sph2s'))")
     r = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_config_states_whether_the_step_data_exceeds_l2():
+    """Timed steps need inputs larger than L2 or a flush between them: the headline
+    2M case says it exceeds L2, the 32,768-particle parity case says it fits; both arms
+    emit the same config for the same workload."""
+    big, d1 = bench.workload_reference("c1")
+    small, d0 = bench.workload_reference("c0")
+    assert "> L2, no flush needed" in bench.config_for(d1, 1, big)["l2"]
+    assert "fits in L2" in bench.config_for(d0, 1, small)["l2"]
+    ours, d = bench.workload("c0")
+    assert bench.config_for(d, 1, ours) == bench.config_for(d0, 1, small)
