@@ -778,9 +778,9 @@ def run_ours(args):
     # kernels per step: from 131,072 particles the step sorts coherently (keys and
     # flags, offsets, compaction, digit offsets, the passes, placement, cell
     # ranges), below from scratch (hash, digit offsets, the passes, gather);
-    # then density and force
+    # then the boundary force pass beside density, density and force
     coherent = sc.fluid.num_particles >= 131072
-    launches = ((8 if coherent else 5) + passes) * args.steps
+    launches = ((9 if coherent else 6) + passes) * args.steps
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

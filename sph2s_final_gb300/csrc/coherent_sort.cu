@@ -307,7 +307,8 @@ __global__ void __launch_bounds__(256) coherent_cells_kernel(const uint32_t* __r
                                                              uint32_t n, GridParams g,
                                                              uint2* __restrict__ cells,
                                                              uint32_t* __restrict__ kprev,
-                                                             uint32_t* __restrict__ err) {
+                                                             uint32_t* __restrict__ err,
+                                                             NearList near) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t key = keys[i];
@@ -322,6 +323,7 @@ __global__ void __launch_bounds__(256) coherent_cells_kernel(const uint32_t* __r
         atomicOr(err, 2u);
         return;
     }
+    near_append(near, c, i);
     const uint32_t prev = i > 0 ? keys[i - 1] : 0u;
     if (i == 0 || prev != key) {
         cw[2 * c] = i;
@@ -403,13 +405,13 @@ void coherent_reset(const CoherentSort& c, cudaStream_t st) {
 void coherent_sort_cells(const CoherentSort& c, const float4* pos, const float4* vel,
                          const GridParams& g, uint2* cells, int key_bits, uint32_t* keys,
                          uint32_t* keys_out, uint32_t* perm_out, float4* pos_out, float4* vel_out,
-                         uint32_t* err, int force_timeout, cudaStream_t st) {
+                         uint32_t* err, int force_timeout, cudaStream_t st, NearList near) {
     coherent_run(c, pos, &g, cells, keys, key_bits, keys_out, perm_out, pos, vel, pos_out, vel_out,
                  err, force_timeout, st);
     if (c.n == 0) return;
     cudaMemsetAsync(cells, 0xFF, sizeof(uint2) * (size_t)g.dx * g.dy * g.dz, st);
     coherent_cells_kernel<<<(c.n + 255) / 256, 256, 0, st>>>(keys_out, c.n, g, cells, c.kprev,
-                                                              err);
+                                                              err, near);
 }
 
 void coherent_sort_keys(const CoherentSort& c, const uint32_t* keys, int key_bits,

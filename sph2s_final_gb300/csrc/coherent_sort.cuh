@@ -62,11 +62,13 @@ void coherent_reset(const CoherentSort& c, cudaStream_t st);
 // `cells` is read first: if it is the table of the last call (the one built
 // with kprev), placing the particles that changed cell is a lookup; every
 // entry is checked against kprev before use, so a stale or garbage table is
-// safe.
+// safe.  With near.list, the sorted indices of the particles whose cell is
+// flagged in near.bnear are appended to it (near.count zeroed beforehand).
 void coherent_sort_cells(const CoherentSort& c, const float4* pos, const float4* vel,
                          const GridParams& g, uint2* cells, int key_bits, uint32_t* keys,
                          uint32_t* keys_out, uint32_t* perm_out, float4* pos_out, float4* vel_out,
-                         uint32_t* err, int force_timeout, cudaStream_t st);
+                         uint32_t* err, int force_timeout, cudaStream_t st,
+                         NearList near = NearList{});
 
 // The same for keys already in memory (n = c.n keys); kprev is read, not
 // written.

@@ -172,6 +172,31 @@ __device__ __forceinline__ DepthClass depth_class(const GridParams& g, float x, 
     return {(uint32_t)c, __fmul_rn(c, quantum)};
 }
 
+// Particles whose cell has boundary particles within stencil reach, listed
+// by the kernel that builds the step's cell ranges (sorted index, in no
+// particular order) for the step's boundary force pass.
+struct NearList {
+    const uint8_t* bnear = nullptr;  // per cell (static); nullptr: no list
+    uint32_t* list = nullptr;        // capacity n
+    uint32_t* count = nullptr;       // zeroed before the kernel
+};
+
+// Appends sorted index i if its cell c is near the boundary: one atomic per
+// warp, each lane's slot from its rank among the appending lanes.
+__device__ __forceinline__ void near_append(const NearList& L, uint32_t c, uint32_t i) {
+    if (!L.list) return;
+    const bool want = L.bnear[c] != 0;
+    const uint32_t am = __activemask();
+    const uint32_t b = __ballot_sync(am, want);
+    if (!b) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = (uint32_t)__ffs(b) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(L.count, (uint32_t)__popc(b));
+    base = __shfl_sync(am, base, (int)leader);
+    if (want) L.list[base + (uint32_t)__popc(b & ((1u << lane) - 1u))] = i;
+}
+
 // Boundary weight shape of evaluateBoundaryWeight (Solver.cu:169-196)
 // without the 0.02 c^2 / r factor: q = 2r/h.
 __device__ __forceinline__ float boundary_shape(float q) {

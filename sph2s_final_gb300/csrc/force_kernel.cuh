@@ -6,6 +6,14 @@
 // neighbour costs two 16-byte gathers, xa[j] = (x, p/rho^2) and
 // va[j] = (v, 1/rho) (the step's velocity array with 1/rho in w), and the next
 // group of four indices is fetched while the current group is processed.
+//
+// The boundary force needs only the step's sorted positions, so the step
+// computes it in boundary_force_kernel, on a second graph branch that runs
+// beside the density pass, for the particles whose cell has boundary particles
+// within stencil reach; the force pass then loads those sums (BSEP).  Inside
+// the force pass the boundary stencil scan of a few near-wall lanes held their
+// whole warps: ~21 % of the pass at 2M particles on GB300.  The sums are the
+// same bit for bit (same loop, same positions).
 #pragma once
 #include "common.cuh"
 
@@ -33,19 +41,126 @@ __device__ __forceinline__ void force_pair(ForceAcc& A, const SimParams& P, floa
     A.wz = fmaf(vc, vj.z - vi.z, A.wz);
 }
 
+// One boundary particle's term: true (and accumulated) if it lies within h.
+__device__ __forceinline__ bool boundary_pair(const float4& xi, const float4& xj,
+                                              const SimParams& P, float& bx, float& by,
+                                              float& bz) {
+    float dx, dy, dz;
+    const float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
+    if (!(r2 < P.T)) return false;
+    const float rs = rsqrtf(r2);
+    const float q = r2 * rs * P.two_over_h;
+    const float w = P.bnd_coef * boundary_shape(q) * rs * rs;
+    bx = fmaf(w, dx, bx);
+    by = fmaf(w, dy, by);
+    bz = fmaf(w, dz, bz);
+    return true;
+}
+
+// Boundary force on a fluid particle at xi (computeBoundaryForceCell,
+// Solver.cu:300-344, scaled by m_b / (m + m_b)): every boundary particle of
+// the stencil within h, each cell's scan cut at the depth boundary_reach
+// allows; COUNT also counts them.  MASKED: `mask` has bit
+// (dz+1)*9 + (dy+1)*3 + (dx+1) set for each cell home + (dx, dy, dz) of the
+// grid that holds boundary particles, and stencil cells within one cell of
+// the home cell (hx, hy, hz) whose bit is clear are skipped (they hold none).
+template <bool COUNT, bool MASKED = false>
+__device__ __forceinline__ void boundary_sum(const float4& xi, const float4* __restrict__ bpos,
+                                             const uint2* __restrict__ bcells, uint32_t nb,
+                                             const SimParams& P, float& bx, float& by, float& bz,
+                                             uint32_t& bcnt, uint32_t mask = 0u, int hx = 0,
+                                             int hy = 0, int hz = 0) {
+    const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+    const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
+    for (int cz = s.z0; cz <= s.z1; ++cz)
+        for (int cy = s.y0; cy <= s.y1; ++cy) {
+            const uint32_t row = linear_cell(P.g, 0, cy, cz);
+            for (int cx = s.x0; cx <= s.x1; ++cx) {
+                if (MASKED) {
+                    const uint32_t ox = (uint32_t)(cx - hx + 1), oy = (uint32_t)(cy - hy + 1),
+                                   oz = (uint32_t)(cz - hz + 1);
+                    if (ox < 3u && oy < 3u && oz < 3u && !((mask >> (oz * 9u + oy * 3u + ox)) & 1u))
+                        continue;
+                }
+                const uint2 r = __ldg(&bcells[row + cx]);
+                const uint32_t e = min(r.y, nb);
+                for (uint32_t j = r.x; j < e; ++j) {
+                    const float4 xj = __ldg(&bpos[j]);
+                    if (xj.w >= reach) break;  // the rest of the cell lies deeper
+                    if (boundary_pair(xi, xj, P, bx, by, bz) && COUNT) ++bcnt;
+                }
+            }
+        }
+}
+
+// The particle's home cell in the linear cell table.
+__device__ __forceinline__ uint32_t home_cell(const GridParams& g, const float4& xi) {
+    return linear_cell(g, cell_coord(xi.x, g.ox, g.spacing, g.dx),
+                       cell_coord(xi.y, g.oy, g.spacing, g.dy),
+                       cell_coord(xi.z, g.oz, g.spacing, g.dz));
+}
+
+// Boundary sums of the particles listed by the cell-range kernel (those whose
+// cell has boundary particles within stencil reach, bnear), for the force
+// pass to load: bacc[i] = (b, 0).  Grid-stride over the list.  A particle
+// inside the grid's box whose stencil is its home cell +-1 (clamped) walks
+// the home cell's static candidate list (bcand[bstart[c] .. bstart[c+1]):
+// the boundary particles of those cells, in stencil order, that lie within
+// h plus a margin of the cell's box, a superset of every such particle's
+// boundary neighbours in the order of the full scan), whose loads do not
+// depend on one another; any other particle scans the stencil, skipping the
+// adjacent cells that hold no boundary particles (bmask).  Both give the
+// full scan's sum bit for bit.
+static __global__ void __launch_bounds__(256) boundary_force_kernel(
+    const float4* __restrict__ pos, const float4* __restrict__ bpos,
+    const uint2* __restrict__ bcells, const uint32_t* __restrict__ bmask,
+    const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcand,
+    const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t n,
+    uint32_t nb, SimParams P, float4* __restrict__ bacc) {
+    const uint32_t cnt = min(*count, n);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
+        const uint32_t i = min(list[t], n - 1);
+        const float4 xi = pos[i];
+        const int hx = cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx);
+        const int hy = cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy);
+        const int hz = cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz);
+        const uint32_t home = linear_cell(P.g, hx, hy, hz);
+        float bx = 0.f, by = 0.f, bz = 0.f;
+        const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+        const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&
+                            xi.z >= P.g.oz && xi.z < P.g.ez;
+        if (inside && S.x0 == max(hx - 1, 0) && S.x1 == min(hx + 1, P.g.dx - 1) &&
+            S.y0 == max(hy - 1, 0) && S.y1 == min(hy + 1, P.g.dy - 1) &&
+            S.z0 == max(hz - 1, 0) && S.z1 == min(hz + 1, P.g.dz - 1)) {
+            const uint32_t e = __ldg(&bstart[home + 1]);
+            for (uint32_t k = __ldg(&bstart[home]); k < e; ++k) {
+                const uint32_t j = min(__ldg(&bcand[k]), nb - 1);
+                boundary_pair(xi, __ldg(&bpos[j]), P, bx, by, bz);
+            }
+        } else {
+            uint32_t c = 0;
+            boundary_sum<false, true>(xi, bpos, bcells, nb, P, bx, by, bz, c, __ldg(&bmask[home]),
+                                      hx, hy, hz);
+        }
+        bacc[i] = make_float4(bx, by, bz, 0.0f);
+    }
+}
+
 // Pressure (spiky gradient), viscosity (Laplacian), tension (Poly6), boundary
 // force and gravity; MODE 0 integrates (symplectic Euler) into pos_out/vel_out,
 // MODE 1 writes the acceleration and the boundary neighbour count instead.
 // Particle i of the sorted array; cells/bcells/bnear are the particle's own
-// grid tables (the batched solver passes per-scene tables and P).
-template <int MODE>
+// grid tables (the batched solver passes per-scene tables and P).  BSEP: the
+// boundary sums were computed by boundary_force_kernel into bacc.
+template <int MODE, bool BSEP = false>
 __device__ __forceinline__ void force_one(
     uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ xa,
     const float4* __restrict__ va, const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     const SimParams& P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
+    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b,
+    const float4* __restrict__ bacc = nullptr) {
     const float4 xi = xa[i];  // (x, y, z, p/rho^2)
     const float4 vi = va[i];  // (v, 1/rho)
     const float tcoef = P.tens_coef * vi.w;
@@ -93,35 +208,15 @@ __device__ __forceinline__ void force_one(
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
     uint32_t bcnt = 0;
-    const uint32_t home = linear_cell(P.g, cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx),
-                                      cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy),
-                                      cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz));
-    if (__ldg(&bnear[home])) {
-        const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
-        const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
-        for (int cz = s.z0; cz <= s.z1; ++cz)
-            for (int cy = s.y0; cy <= s.y1; ++cy) {
-                const uint32_t row = linear_cell(P.g, 0, cy, cz);
-                for (int cx = s.x0; cx <= s.x1; ++cx) {
-                    const uint2 r = __ldg(&bcells[row + cx]);
-                    const uint32_t e = min(r.y, nb);
-                    for (uint32_t j = r.x; j < e; ++j) {
-                        const float4 xj = __ldg(&bpos[j]);
-                        if (xj.w >= reach) break;  // the rest of the cell lies deeper
-                        float dx, dy, dz;
-                        float r2 = dist2(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z, dx, dy, dz);
-                        if (r2 < P.T) {
-                            float rs = rsqrtf(r2);
-                            float q = r2 * rs * P.two_over_h;
-                            float w = P.bnd_coef * boundary_shape(q) * rs * rs;
-                            bx = fmaf(w, dx, bx);
-                            by = fmaf(w, dy, by);
-                            bz = fmaf(w, dz, bz);
-                            if (MODE == 1) ++bcnt;
-                        }
-                    }
-                }
-            }
+    if (__ldg(&bnear[home_cell(P.g, xi)])) {
+        if (BSEP) {
+            const float4 b = bacc[i];
+            bx = b.x;
+            by = b.y;
+            bz = b.z;
+        } else {
+            boundary_sum<MODE == 1>(xi, bpos, bcells, nb, P, bx, by, bz, bcnt);
+        }
     }
     const float vf = P.visc_coef * vi.w;
     const float axx = fmaf(vf, A.wx, A.fx) + bx;
@@ -140,18 +235,19 @@ __device__ __forceinline__ void force_one(
     }
 }
 
-template <int MODE>
+template <int MODE, bool BSEP = false>
 __global__ void __launch_bounds__(256, 6) force_kernel(
     const float4* __restrict__ pos, const float4* __restrict__ xa, const float4* __restrict__ va,
     const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     SimParams P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b) {
+    float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b,
+    const float4* __restrict__ bacc = nullptr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    force_one<MODE>(i, pos, xa, va, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P, dt,
-                    pos_out, vel_out, acc_out, nbr_b);
+    force_one<MODE, BSEP>(i, pos, xa, va, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P,
+                          dt, pos_out, vel_out, acc_out, nbr_b, bacc);
 }
 
 }  // namespace sph

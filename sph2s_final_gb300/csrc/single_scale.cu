@@ -4,11 +4,13 @@
 // the handle owns all device memory, keeps its configuration in kernel
 // parameters instead of one __constant__ symbol, runs on its own stream, and
 // captures one step into a CUDA graph that is replayed by sph_advance.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 #include "errors.h"
 #include "host_params.h"
+#include "scan.cuh"
 #include "single_scale_kernels.cuh"
 
 using namespace sph;
@@ -27,9 +29,13 @@ int free_solver(sph_solver* s) {
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->co_mem,  s->err,   s->stage, s->nbr, s->nbr_count,
-                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa};
+                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa, s->bacc, s->bmask, s->blist, s->bcount, s->bstart, s->bcand};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (s->side) cudaStreamSynchronize(s->side);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
     for (int b = 0; b < 2; ++b) {
         if (s->astage[b]) cudaFree(s->astage[b]);
@@ -62,6 +68,11 @@ int enqueue_neighborhood(sph_solver* s) {
     int out = 1;
     const bool coherent = s->sort_mode == kSortCoherent ||
                           (s->sort_mode == kSortAuto && s->n >= kCoherentMinParticles);
+    NearList near;  // the near-boundary particles, for the boundary force pass
+    near.bnear = s->bnear;
+    near.list = s->blist;
+    near.count = s->bcount;
+    cudaMemsetAsync(s->bcount, 0, 4, st);
     if (!coherent || s->force_timeout) {
         const int passes = sort_passes(s->key_bits);
         sort_reset(s->sort, st);
@@ -72,26 +83,38 @@ int enqueue_neighborhood(sph_solver* s) {
         out = sort_passes_run(s->keys, s->vals, nullptr, s->n, passes, s->sort, s->err, s->force_timeout, st);
     } else {  // sort, reorder and cell table in one sequence
         coherent_sort_cells(s->co, s->pos, s->vel, s->P.g, s->cells, s->key_bits, s->keys[0],
-                            s->keys[1], s->vals[1], s->spos, s->svel, s->err, s->force_timeout, st);
+                            s->keys[1], s->vals[1], s->spos, s->svel, s->err, s->force_timeout, st,
+                            near);
         return out;
     }
     cudaMemsetAsync(s->cells, 0xFF, sizeof(uint2) * s->ncells, st);
     gather_cells_kernel<true><<<blocks_for(s->n), 256, 0, st>>>(
         s->keys[out], s->vals[out], s->n, s->P.g, s->pos, s->vel, s->spos, s->svel, s->cells,
-        s->err, 0, s->co.kprev);
+        s->err, 0, s->co.kprev, near);
     return out;
 }
 
+// The density pass, and beside it on the second branch (fork/join events,
+// captured into the step graph as a parallel branch) the boundary force sums
+// of the near-boundary particles, which need only the sorted positions.
 void enqueue_density(sph_solver* s) {
+    cudaEventRecord(s->fork, s->stream);
+    cudaStreamWaitEvent(s->side, s->fork, 0);
+    const uint32_t bgrid = std::min(blocks_for(s->n), (uint32_t)(2 * (s->sms > 0 ? s->sms : 1)));
+    boundary_force_kernel<<<bgrid, 256, 0, s->side>>>(s->spos, s->bpos, s->bcells, s->bmask,
+                                                      s->bstart, s->bcand, s->blist, s->bcount,
+                                                      s->n, s->nb, s->P, s->bacc);
+    cudaEventRecord(s->join, s->side);
     density_kernel<false><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
         s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, nullptr, s->xa,
         s->svel);
 }
 
 void enqueue_force(sph_solver* s, float dt) {
-    force_kernel<0><<<blocks_for(s->n), 256, 0, s->stream>>>(
+    cudaStreamWaitEvent(s->stream, s->join, 0);
+    force_kernel<0, true><<<blocks_for(s->n), 256, 0, s->stream>>>(
         s->spos, s->xa, s->svel, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
-        s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr);
+        s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr, s->bacc);
 }
 
 // One step: Solver::Advance (Solver.cu:1082-1096) with integrate fused into
@@ -174,6 +197,9 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
         }                           \
     } while (0)
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming), "event", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming), "event", __FILE__, __LINE__));
     uint32_t nmax = n_fluid > n_boundary ? n_fluid : n_boundary;
     TRY(dalloc(&s->pos, n_fluid));
     TRY(dalloc(&s->vel, n_fluid));
@@ -185,6 +211,16 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
     TRY(dalloc(&s->nbr, (size_t)n_fluid * (kMaxNbr / 4)));
     TRY(dalloc(&s->nbr_count, n_fluid));
     TRY(dalloc(&s->bnear, s->ncells));
+    TRY(dalloc(&s->bacc, n_fluid));
+    TRY(check_cuda(cudaMemsetAsync(s->bacc, 0, sizeof(float4) * (n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
+    TRY(dalloc(&s->bmask, s->ncells));
+    TRY(dalloc(&s->blist, n_fluid));
+    TRY(dalloc(&s->bcount, 1));
+    {
+        int dev = 0;
+        TRY(check_cuda(cudaGetDevice(&dev), "device", __FILE__, __LINE__));
+        TRY(check_cuda(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev), "device", __FILE__, __LINE__));
+    }
     TRY(dalloc(&s->keys[0], nmax));
     TRY(dalloc(&s->keys[1], nmax));
     TRY(dalloc(&s->vals[0], nmax));
@@ -276,7 +312,28 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
         const int reach = (int)std::ceil(config->effective_radius / config->grid.spacing) + 1;
         boundary_near_kernel<<<blocks_for(s->ncells), 256, 0, s->stream>>>(s->bcells, s->P.g, reach,
                                                                            s->bnear);
+        boundary_mask_kernel<<<blocks_for(s->ncells), 256, 0, s->stream>>>(s->bcells, s->P.g,
+                                                                           s->bmask);
         TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
+        // static boundary candidates of the near cells: count, prefix sum, fill
+        TRY(dalloc(&s->bstart, (size_t)s->ncells + 1));
+        TRY(check_cuda(cudaMemsetAsync(s->bstart + s->ncells, 0, 4, s->stream), "memset", __FILE__, __LINE__));
+        const float lim = s->P.h * 1.01f + 4.0f * s->P.bmargin;
+        boundary_cand_kernel<false><<<blocks_for(s->ncells), 256, 0, s->stream>>>(
+            s->bcells, s->bpos, s->bnear, s->P.g, n_boundary, lim, s->bstart, nullptr);
+        uint32_t* scratch = nullptr;
+        TRY(dalloc(&scratch, scan_scratch_words(s->ncells + 1)));
+        const ScanSeg seg = {s->bstart, s->bstart, s->ncells + 1, s->bcount};
+        scan_exclusive_batch(&seg, 1, scratch, s->stream);
+        uint32_t total = 0;
+        cudaError_t e = cudaMemcpyAsync(&total, s->bcount, 4, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        cudaFree(scratch);
+        TRY(check_cuda(e, "boundary candidates", __FILE__, __LINE__));
+        TRY(dalloc(&s->bcand, total));
+        boundary_cand_kernel<true><<<blocks_for(s->ncells), 256, 0, s->stream>>>(
+            s->bcells, s->bpos, s->bnear, s->P.g, n_boundary, lim, s->bstart, s->bcand);
+        TRY(check_cuda(cudaGetLastError(), "boundary candidates", __FILE__, __LINE__));
         TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
     }
     TRY(check_device_error(s));

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     GridParams g, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr) {
+    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr,
+    NearList near = NearList{}) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (kprev_out) kprev_out[i] = keys_sorted[i];  // the next step's coherent sort starts here
@@ -91,6 +92,7 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
         atomicOr(err, 2u);
         return;
     }
+    near_append(near, c, i);
     const uint32_t prev = i > 0 ? keys_sorted[i - 1] >> key_shift : 0u;
     if (i == 0 || prev != key) {
         cw[2 * c] = i;
@@ -170,6 +172,73 @@ static __global__ void __launch_bounds__(256) boundary_near_kernel(const uint2* 
                 }
             }
     near[c] = f;
+}
+
+// Per cell, the adjacent cells (offsets -1..1 per axis, bit (dz+1)*9 +
+// (dy+1)*3 + (dx+1)) that lie in the grid and hold boundary particles.
+static __global__ void __launch_bounds__(256) boundary_mask_kernel(const uint2* __restrict__ bcells,
+                                                                   GridParams g,
+                                                                   uint32_t* __restrict__ mask) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nc = (uint32_t)g.dx * g.dy * g.dz;
+    if (c >= nc) return;
+    const int cx = (int)(c % (uint32_t)g.dx);
+    const int cy = (int)((c / (uint32_t)g.dx) % (uint32_t)g.dy);
+    const int cz = (int)(c / ((uint32_t)g.dx * g.dy));
+    uint32_t m = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int x = cx + dx, y = cy + dy, z = cz + dz;
+                if (x < 0 || y < 0 || z < 0 || x >= g.dx || y >= g.dy || z >= g.dz) continue;
+                const uint2 r = bcells[linear_cell(g, x, y, z)];
+                if (r.x != kEmptyCell && r.x < r.y) m |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
+            }
+    mask[c] = m;
+}
+
+// Static boundary candidates of each cell flagged in `near`: the boundary
+// particles of the cells c +-1 (clamped), in stencil order (z, y, x, then the
+// cell's presorted order), whose distance to the cell's box is at most lim.
+// FILL = false counts them into cnt[c]; FILL = true writes their indices
+// from start[c] on.
+template <bool FILL>
+static __global__ void __launch_bounds__(256) boundary_cand_kernel(
+    const uint2* __restrict__ bcells, const float4* __restrict__ bpos,
+    const uint8_t* __restrict__ near, GridParams g, uint32_t nb, float lim,
+    uint32_t* __restrict__ cnt_or_start, uint32_t* __restrict__ cand) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nc = (uint32_t)g.dx * g.dy * g.dz;
+    if (c >= nc) return;
+    if (!near[c]) {
+        if (!FILL) cnt_or_start[c] = 0;
+        return;
+    }
+    const int cx = (int)(c % (uint32_t)g.dx);
+    const int cy = (int)((c / (uint32_t)g.dx) % (uint32_t)g.dy);
+    const int cz = (int)(c / ((uint32_t)g.dx * g.dy));
+    const float lx = g.ox + cx * g.spacing, hx = g.ox + (cx + 1) * g.spacing;
+    const float ly = g.oy + cy * g.spacing, hy = g.oy + (cy + 1) * g.spacing;
+    const float lz = g.oz + cz * g.spacing, hz = g.oz + (cz + 1) * g.spacing;
+    const float lim2 = lim * lim;
+    uint32_t k = FILL ? cnt_or_start[c] : 0u;
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dz - 1); ++z)
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dy - 1); ++y)
+            for (int x = max(cx - 1, 0); x <= min(cx + 1, g.dx - 1); ++x) {
+                const uint2 r = bcells[linear_cell(g, x, y, z)];
+                const uint32_t e = min(r.y, nb);
+                for (uint32_t j = r.x; j < e; ++j) {
+                    const float4 b = bpos[j];
+                    const float dx = fmaxf(fmaxf(lx - b.x, b.x - hx), 0.0f);
+                    const float dy = fmaxf(fmaxf(ly - b.y, b.y - hy), 0.0f);
+                    const float dz = fmaxf(fmaxf(lz - b.z, b.z - hz), 0.0f);
+                    if (dx * dx + dy * dy + dz * dz <= lim2) {
+                        if (FILL) cand[k] = j;
+                        ++k;
+                    }
+                }
+            }
+    if (!FILL) cnt_or_start[c] = k;
 }
 
 }  // namespace sph

@@ -27,6 +27,15 @@ struct sph_solver {
     uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
     uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
     uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
+    uint32_t* bmask = nullptr;      // per cell: adjacent cells holding boundary particles (27 bits)
+    uint32_t* bstart = nullptr;     // per cell + 1: start of its static boundary candidates ...
+    uint32_t* bcand = nullptr;      // ... (boundary particle indices, boundary_cand_kernel)
+    float4* bacc = nullptr;         // boundary force sums of near-boundary particles (step order)
+    uint32_t* blist = nullptr;      // the step's near-boundary particles (sorted indices) ...
+    uint32_t* bcount = nullptr;     // ... and their number
+    int sms = 0;                    // SM count (grid of the boundary force pass)
+    cudaStream_t side = nullptr;    // second branch of the step: the boundary force
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
     uint2* cells = nullptr;
