@@ -102,7 +102,9 @@ __device__ __forceinline__ uint32_t home_cell(const GridParams& g, const float4&
 
 // Boundary sums of the particles listed by the cell-range kernel (those whose
 // cell has boundary particles within stencil reach, bnear), for the force
-// pass to load: bacc[i] = (b, 0).  Grid-stride over the list.  A particle
+// pass to load: bacc[i] = (b, 0).  Grid-stride over the list, or, without a
+// list, over all n particles, skipping those whose cell is not flagged in
+// near_all (P.g is the grid of the boundary tables).  A particle
 // inside the grid's box whose stencil is its home cell +-1 (clamped) walks
 // the home cell's static candidate list (bcand[bstart[c] .. bstart[c+1]):
 // the boundary particles of those cells, in stencil order, that lie within
@@ -116,15 +118,17 @@ static __global__ void __launch_bounds__(256) boundary_force_kernel(
     const uint2* __restrict__ bcells, const uint32_t* __restrict__ bmask,
     const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcand,
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t n,
-    uint32_t nb, SimParams P, float4* __restrict__ bacc) {
-    const uint32_t cnt = min(*count, n);
+    uint32_t nb, SimParams P, float4* __restrict__ bacc,
+    const uint8_t* __restrict__ near_all = nullptr) {
+    const uint32_t cnt = list ? min(*count, n) : n;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
-        const uint32_t i = min(list[t], n - 1);
+        const uint32_t i = list ? min(list[t], n - 1) : t;
         const float4 xi = pos[i];
         const int hx = cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx);
         const int hy = cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy);
         const int hz = cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz);
         const uint32_t home = linear_cell(P.g, hx, hy, hz);
+        if (!list && !__ldg(&near_all[home])) continue;
         float bx = 0.f, by = 0.f, bz = 0.f;
         const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
         const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&

@@ -10,8 +10,7 @@
 #include <vector>
 #include "errors.h"
 #include "host_params.h"
-#include "scan.cuh"
-#include "single_scale_kernels.cuh"
+#include "boundary_tables.cuh"
 
 using namespace sph;
 
@@ -213,7 +212,6 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
     TRY(dalloc(&s->bnear, s->ncells));
     TRY(dalloc(&s->bacc, n_fluid));
     TRY(check_cuda(cudaMemsetAsync(s->bacc, 0, sizeof(float4) * (n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
-    TRY(dalloc(&s->bmask, s->ncells));
     TRY(dalloc(&s->blist, n_fluid));
     TRY(dalloc(&s->bcount, 1));
     {
@@ -312,28 +310,14 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
         const int reach = (int)std::ceil(config->effective_radius / config->grid.spacing) + 1;
         boundary_near_kernel<<<blocks_for(s->ncells), 256, 0, s->stream>>>(s->bcells, s->P.g, reach,
                                                                            s->bnear);
-        boundary_mask_kernel<<<blocks_for(s->ncells), 256, 0, s->stream>>>(s->bcells, s->P.g,
-                                                                           s->bmask);
         TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
-        // static boundary candidates of the near cells: count, prefix sum, fill
-        TRY(dalloc(&s->bstart, (size_t)s->ncells + 1));
-        TRY(check_cuda(cudaMemsetAsync(s->bstart + s->ncells, 0, 4, s->stream), "memset", __FILE__, __LINE__));
-        const float lim = s->P.h * 1.01f + 4.0f * s->P.bmargin;
-        boundary_cand_kernel<false><<<blocks_for(s->ncells), 256, 0, s->stream>>>(
-            s->bcells, s->bpos, s->bnear, s->P.g, n_boundary, lim, s->bstart, nullptr);
-        uint32_t* scratch = nullptr;
-        TRY(dalloc(&scratch, scan_scratch_words(s->ncells + 1)));
-        const ScanSeg seg = {s->bstart, s->bstart, s->ncells + 1, s->bcount};
-        scan_exclusive_batch(&seg, 1, scratch, s->stream);
-        uint32_t total = 0;
-        cudaError_t e = cudaMemcpyAsync(&total, s->bcount, 4, cudaMemcpyDeviceToHost, s->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        cudaFree(scratch);
-        TRY(check_cuda(e, "boundary candidates", __FILE__, __LINE__));
-        TRY(dalloc(&s->bcand, total));
-        boundary_cand_kernel<true><<<blocks_for(s->ncells), 256, 0, s->stream>>>(
-            s->bcells, s->bpos, s->bnear, s->P.g, n_boundary, lim, s->bstart, s->bcand);
-        TRY(check_cuda(cudaGetLastError(), "boundary candidates", __FILE__, __LINE__));
+        BoundaryTables bt;
+        const cudaError_t e = build_boundary_tables(s->bcells, s->bpos, s->bnear, s->P.g, s->ncells,
+                                                    n_boundary, s->P.h, s->P.bmargin, s->stream, bt);
+        s->bmask = bt.mask;
+        s->bstart = bt.start;
+        s->bcand = bt.cand;
+        TRY(check_cuda(e, "boundary tables", __FILE__, __LINE__));
         TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
     }
     TRY(check_device_error(s));

@@ -17,6 +17,7 @@
 #include "host_params.h"
 #include "radix_sort.cuh"
 #include "scan.cuh"
+#include "boundary_tables.cuh"
 #include "single_scale_kernels.cuh"
 #include "two_scale_kernels.cuh"
 
@@ -43,6 +44,7 @@ struct Pop {
     uint32_t* list_count = nullptr;
     uint4* clist = nullptr;          // complementary force neighbours, ComplCap per particle
     uint32_t* clist_count = nullptr;
+    float4* bacc = nullptr;          // boundary force sums of the step (boundary_force_kernel)
 };
 
 template <class T>
@@ -65,6 +67,11 @@ struct sph_solver2 {
     float4* bpos = nullptr;
     uint2* bcells = nullptr;
     uint8_t* bnear = nullptr;  // per LOW cell: a boundary particle within stencil reach
+    BoundaryTables btab;       // static tables of the boundary force pass (LOW grid)
+    SimParams BP;              // the boundary force's constants: LOW grid, h, threshold, weights
+    int sms = 0;
+    cudaStream_t side = nullptr;  // second branch of the step: the boundary force
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
     void* sort_mem = nullptr;
@@ -95,7 +102,13 @@ namespace {
 int free_solver2(sph_solver2* s) {
     if (!s) return SPH_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->side) cudaStreamSynchronize(s->side);
     for (void* p : s->owned) cudaFree(p);
+    for (void* p : {(void*)s->btab.mask, (void*)s->btab.start, (void*)s->btab.cand})
+        if (p) cudaFree(p);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->ctl_host) cudaFreeHost(s->ctl_host);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -168,7 +181,7 @@ int alloc_pop(Pop& p, uint32_t cap, const sph_grid& g, uint32_t compl_cap, std::
         (rc = dalloc(&p.list, (size_t)cap * (kMaxNbr / 4), o)) ||
         (rc = dalloc(&p.list_count, cap, o)) ||
         (rc = dalloc(&p.clist, (size_t)cap * (compl_cap / 4), o)) ||
-        (rc = dalloc(&p.clist_count, cap, o)))
+        (rc = dalloc(&p.clist_count, cap, o)) || (rc = dalloc(&p.bacc, cap, o)))
         return rc;
     return SPH_OK;
 }
@@ -232,6 +245,19 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
     cudaMemsetAsync(s->ctl + kCtlFadedL, 0, 8, st);
     ts_neighborhoods(s);
     Pop &L = s->pop[0], &H = s->pop[1];
+    // the boundary force sums of both populations on the second branch, beside
+    // the density passes (they need only the sorted positions)
+    const bool bsep = !debug;
+    if (bsep) {
+        cudaEventRecord(s->fork, st);
+        cudaStreamWaitEvent(s->side, s->fork, 0);
+        for (Pop* p : {&H, &L})
+            if (p->n)
+                boundary_force_kernel<<<blocks_for(p->n), 256, 0, s->side>>>(
+                    p->spos, s->bpos, s->bcells, s->btab.mask, s->btab.start, s->btab.cand,
+                    nullptr, nullptr, p->n, s->nb, s->BP, p->bacc, s->bnear);
+        cudaEventRecord(s->join, s->side);
+    }
     if (H.n) {
         if (debug && dbg_pop == 1)
             ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
@@ -259,27 +285,28 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
     else if (gb)
         cudaMemsetAsync(s->gmerge, 0, 4 * (size_t)gb, st);
     const uint32_t* gm = gb ? s->gmerge : nullptr;
+    if (bsep) cudaStreamWaitEvent(st, s->join, 0);
     if (H.n) {
         TSOut o = outputs(H, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[1] : nullptr);
         if (debug && dbg_pop == 1)
             ts_force_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
+                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o, nullptr);
         else
             ts_force_kernel<1, false><<<blocks_for(H.n), 256, 0, st>>>(
                 H.spos, H.svel, H.sstt, H.sgrp, H.aux, H.cells, H.n, L.spos, L.svel, L.aux, L.cells,
-                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o);
+                L.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, H.rho, H.list, H.list_count, H.clist, H.clist_count, o, bsep ? H.bacc : nullptr);
     }
     if (L.n) {
         TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
             ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
+                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o, nullptr);
         else
             ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
-                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o);
+                H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o, bsep ? L.bacc : nullptr);
     }
 }
 
@@ -410,6 +437,23 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
         return fail(SPH_E_INVALID, "two-scale state: group counter beyond the group capacity");
     }
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming), "event", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming), "event", __FILE__, __LINE__));
+    {
+        int dev = 0;
+        TRY(check_cuda(cudaGetDevice(&dev), "device", __FILE__, __LINE__));
+        TRY(check_cuda(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev), "device", __FILE__, __LINE__));
+    }
+    // the boundary force uses the LOW grid, radius and threshold for both populations
+    s->BP = SimParams{};
+    s->BP.g = P.g[0];
+    s->BP.h = P.h[0];
+    s->BP.h2 = P.h2[0];
+    s->BP.T = P.T[0];
+    s->BP.bnd_coef = P.bnd_coef;
+    s->BP.two_over_h = P.two_over_h0;
+    s->BP.bmargin = P.bmargin;
     TRY(alloc_pop(s->pop[0], (uint32_t)capL, config->grid[0], ComplCap<0>::value, s->owned));
     TRY(alloc_pop(s->pop[1], (uint32_t)capH, config->grid[1], ComplCap<1>::value, s->owned));
     // one sort holds both populations (ts_neighborhoods), or the boundary at creation
@@ -484,6 +528,9 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
         boundary_near_kernel<<<blocks_for(s->pop[0].ncells), 256, 0, s->stream>>>(
             s->bcells, s->P.g[0], reach, s->bnear);
         TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
+        TRY(check_cuda(build_boundary_tables(s->bcells, s->bpos, s->bnear, s->P.g[0], s->pop[0].ncells,
+                                             n_boundary, s->P.h[0], s->P.bmargin, s->stream, s->btab),
+                       "boundary tables", __FILE__, __LINE__));
         TRY(check_cuda(cudaStreamSynchronize(s->stream), "create sync", __FILE__, __LINE__));
     }
     TRY(check_err2(s));

@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     unsigned long long* __restrict__ gacc, uint32_t* __restrict__ ctl,
     const float* __restrict__ rho_r, const uint4* __restrict__ list4,
     const uint32_t* __restrict__ list_count, const uint4* __restrict__ clist4,
-    const uint32_t* __restrict__ clist_count, TSOut out) {
+    const uint32_t* __restrict__ clist_count, TSOut out, const float4* __restrict__ bacc) {
     constexpr int C = 1 - R;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_r) return;
@@ -447,11 +447,20 @@ __global__ void __launch_bounds__(256) ts_force_kernel(
     float bx = 0.f, by = 0.f, bz = 0.f;
     uint32_t bcnt = 0;
     // the boundary stencil lives on the LOW grid; particles of LOW cells with no
-    // boundary particle within stencil reach skip it (bnear, set once at creation)
+    // boundary particle within stencil reach skip it (bnear, set once at creation).
+    // With bacc the step computed the sums beside the density passes
+    // (boundary_force_kernel, the same bits).
     const uint32_t bhome = linear_cell(P.g[0], cell_coord(xi.x, P.g[0].ox, P.g[0].spacing, P.g[0].dx),
                                        cell_coord(xi.y, P.g[0].oy, P.g[0].spacing, P.g[0].dy),
                                        cell_coord(xi.z, P.g[0].oz, P.g[0].spacing, P.g[0].dz));
-    if (__ldg(&bnear[bhome])) {
+    if (!DEBUG && bacc != nullptr) {
+        if (__ldg(&bnear[bhome])) {
+            const float4 b = bacc[i];
+            bx = b.x;
+            by = b.y;
+            bz = b.z;
+        }
+    } else if (__ldg(&bnear[bhome])) {
         const Stencil st = stencil(P.g[0], xi.x, xi.y, xi.z, P.h[0]);
         const float reach = boundary_reach(P.g[0], P.h[0], P.bmargin, xi.x, xi.y, xi.z);
         for (int cz = st.z0; cz <= st.z1; ++cz)
