@@ -15,6 +15,7 @@
 #include "batched_solver.h"
 #include "errors.h"
 #include "host_params.h"
+#include "scan.cuh"
 #include "single_scale_kernels.cuh"
 
 using namespace sph;
@@ -35,9 +36,13 @@ namespace sph_b {
 int free_batch(sph_batch* b) {
     if (!b) return SPH_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->side) cudaStreamSynchronize(b->side);
     sphb_rollout_release(b);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (void* p : b->owned) cudaFree(p);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->err_host) cudaFreeHost(b->err_host);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -70,10 +75,18 @@ template <int BS>
 void launch_force(sph_batch* b, int ti, float dt) {
     b_force_kernel<BS><<<pgrid(b, b->ntiles[ti]), BS, 0, b->stream>>>(
         b->tiles[ti], b->ntiles[ti], b->recs, b->spos, b->xa, b->svel, b->cells, b->nbr,
-        b->nbr_count, b->bpos, b->bcells, b->bnear, b->N, b->NB, dt, b->pos, b->vel);
+        b->nbr_count, b->bpos, b->bcells, b->bnear, b->N, b->NB, dt, b->pos, b->vel, b->bacc);
 }
 
+// The density pass, and beside it on the second branch (fork / join events,
+// a parallel branch of the step graph) the boundary force sums.
 void enqueue_density(sph_batch* b) {
+    cudaEventRecord(b->fork, b->stream);
+    cudaStreamWaitEvent(b->side, b->fork, 0);
+    b_boundary_force_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, b->side>>>(
+        b->tiles[1], b->ntiles[1], b->recs, b->spos, b->bpos, b->bcells, b->bnear, b->bmask,
+        b->bstart, b->bcand, b->NB, b->bacc);
+    cudaEventRecord(b->join, b->side);
     switch (b->bs_density) {
         case 0: launch_density<128>(b, 0); break;
         case 2: launch_density<512>(b, 2); break;
@@ -82,6 +95,7 @@ void enqueue_density(sph_batch* b) {
 }
 
 void enqueue_force(sph_batch* b, float dt) {
+    cudaStreamWaitEvent(b->stream, b->join, 0);
     switch (b->bs_force) {
         case 0: launch_force<128>(b, 0, dt); break;
         case 2: launch_force<512>(b, 2, dt); break;
@@ -210,6 +224,9 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(check_cuda(cudaGetDevice(&dev), "device", __FILE__, __LINE__));
     TRY(check_cuda(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev), "attr", __FILE__, __LINE__));
     TRY(check_cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "event", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "event", __FILE__, __LINE__));
     const uint32_t nmax = std::max(b->N, b->NB);
     TRY(dalloc(&b->recs, num_scenes, b->owned));
     TRY(dalloc(&b->pos, b->N, b->owned));
@@ -230,6 +247,10 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(dalloc(&b->cells, b->NC, b->owned));
     TRY(dalloc(&b->bcells, b->NC, b->owned));
     TRY(dalloc(&b->bnear, b->NC, b->owned));
+    TRY(dalloc(&b->bmask, b->NC, b->owned));
+    TRY(dalloc(&b->bstart, (size_t)b->NC + 1, b->owned));
+    TRY(dalloc(&b->bacc, b->N, b->owned));
+    TRY(check_cuda(cudaMemset(b->bacc, 0, 16 * (size_t)std::max(b->N, 1u)), "memset", __FILE__, __LINE__));
     TRY(dalloc(&b->bpos, b->NB, b->owned));
     TRY(check_cuda(cudaMalloc(&b->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));
     b->owned.push_back(b->sort_mem);
@@ -324,6 +345,44 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
                                                                           reach, b->bnear + R.c_off);
         }
         TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
+        // static boundary tables of every scene (boundary_tables.cuh): masks and
+        // candidate counts per scene, one prefix sum over all cells, then the
+        // candidates (global boundary indices)
+        std::vector<float> lims(num_scenes);
+        for (uint32_t s = 0; s < num_scenes; ++s) {
+            const SceneRec& R = b->recs_h[s];
+            const uint32_t nc = sph_grid_num_cells(&scenes[s].config.grid);
+            lims[s] = R.P.h * 1.01f + 4.0f * R.P.bmargin;
+            if (!nc) continue;
+            boundary_mask_kernel<<<(nc + 255) / 256, 256, 0, b->stream>>>(b->bcells + R.c_off, R.P.g,
+                                                                          b->bmask + R.c_off);
+            boundary_cand_kernel<false><<<(nc + 255) / 256, 256, 0, b->stream>>>(
+                b->bcells + R.c_off, b->bpos, b->bnear + R.c_off, R.P.g, b->NB, lims[s],
+                b->bstart + R.c_off, nullptr);
+        }
+        TRY(check_cuda(cudaMemsetAsync(b->bstart + b->NC, 0, 4, b->stream), "memset", __FILE__, __LINE__));
+        {
+            const uint32_t words = (uint32_t)scan_scratch_words(b->NC + 1);
+            uint32_t* scratch = nullptr;
+            TRY(dalloc(&scratch, (size_t)words + 1, b->owned));
+            const ScanSeg seg = {b->bstart, b->bstart, b->NC + 1, scratch + words};
+            scan_exclusive_batch(&seg, 1, scratch, b->stream);
+            uint32_t total = 0;
+            TRY(check_cuda(cudaMemcpyAsync(&total, scratch + words, 4, cudaMemcpyDeviceToHost, b->stream), "copy", __FILE__, __LINE__));
+            TRY(check_cuda(cudaStreamSynchronize(b->stream), "boundary tables", __FILE__, __LINE__));
+            cudaFree(scratch);
+            b->owned.pop_back();
+            TRY(dalloc(&b->bcand, total, b->owned));
+        }
+        for (uint32_t s = 0; s < num_scenes; ++s) {
+            const SceneRec& R = b->recs_h[s];
+            const uint32_t nc = sph_grid_num_cells(&scenes[s].config.grid);
+            if (!nc) continue;
+            boundary_cand_kernel<true><<<(nc + 255) / 256, 256, 0, b->stream>>>(
+                b->bcells + R.c_off, b->bpos, b->bnear + R.c_off, R.P.g, b->NB, lims[s],
+                b->bstart + R.c_off, b->bcand);
+        }
+        TRY(check_cuda(cudaGetLastError(), "boundary tables", __FILE__, __LINE__));
         TRY(check_cuda(cudaStreamSynchronize(b->stream), "create", __FILE__, __LINE__));
     }
     TRY(check_err(b));

@@ -150,6 +150,34 @@ __global__ void __launch_bounds__(BS) b_density_kernel(
     }
 }
 
+// Boundary force sums of the scenes' near-boundary particles (bnear of the
+// scene's cell), from the scenes' static candidate tables (boundary_force_one),
+// for b_force_kernel to load.
+template <int BS>
+__global__ void __launch_bounds__(BS) b_boundary_force_kernel(
+    const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
+    const float4* __restrict__ pos, const float4* __restrict__ bpos,
+    const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear,
+    const uint32_t* __restrict__ bmask, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, uint32_t nb, float4* __restrict__ bacc) {
+    for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
+        const uint2 tile = tiles[t];
+        const SceneRec& R = recs[tile.x];
+        const uint32_t i = tile.y + threadIdx.x;
+        if (i >= R.p_off + R.p_n) continue;
+        const float4 xi = pos[i];
+        const GridParams& g = R.P.g;
+        const int hx = cell_coord(xi.x, g.ox, g.spacing, g.dx);
+        const int hy = cell_coord(xi.y, g.oy, g.spacing, g.dy);
+        const int hz = cell_coord(xi.z, g.oz, g.spacing, g.dz);
+        const uint32_t home = linear_cell(g, hx, hy, hz);
+        if (!__ldg(&bnear[R.c_off + home])) continue;
+        const SimParams P = R.P;
+        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells + R.c_off, bmask + R.c_off,
+                           bstart + R.c_off, bcand, nb, P, bacc);
+    }
+}
+
 template <int BS>
 __global__ void __launch_bounds__(BS) b_force_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
@@ -157,15 +185,17 @@ __global__ void __launch_bounds__(BS) b_force_kernel(
     const uint2* __restrict__ cells, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
-    float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+    float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+    const float4* __restrict__ bacc) {
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
         const SceneRec& R = recs[tile.x];
         const uint32_t i = tile.y + threadIdx.x;
         if (i >= R.p_off + R.p_n) continue;
         const SimParams P = R.P;
-        force_one<0>(i, pos, xa, va, cells + R.c_off, nbr4, nbr_count, bpos, bcells + R.c_off,
-                     bnear + R.c_off, n, nb, P, dt, pos_out, vel_out, nullptr, nullptr);
+        force_one<0, true>(i, pos, xa, va, cells + R.c_off, nbr4, nbr_count, bpos,
+                           bcells + R.c_off, bnear + R.c_off, n, nb, P, dt, pos_out, vel_out,
+                           nullptr, nullptr, bacc);
     }
 }
 

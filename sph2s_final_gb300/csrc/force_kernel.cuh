@@ -112,7 +112,34 @@ __device__ __forceinline__ uint32_t home_cell(const GridParams& g, const float4&
 // boundary neighbours in the order of the full scan), whose loads do not
 // depend on one another; any other particle scans the stencil, skipping the
 // adjacent cells that hold no boundary particles (bmask).  Both give the
-// full scan's sum bit for bit.
+// full scan's sum bit for bit.  boundary_force_one is the per-particle part
+// (the batched step calls it per scene with that scene's tables).
+__device__ __forceinline__ void boundary_force_one(
+    uint32_t i, const float4& xi, int hx, int hy, int hz, uint32_t home,
+    const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
+    const uint32_t* __restrict__ bmask, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, uint32_t nb, const SimParams& P,
+    float4* __restrict__ bacc) {
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+    const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&
+                        xi.z >= P.g.oz && xi.z < P.g.ez;
+    if (inside && S.x0 == max(hx - 1, 0) && S.x1 == min(hx + 1, P.g.dx - 1) &&
+        S.y0 == max(hy - 1, 0) && S.y1 == min(hy + 1, P.g.dy - 1) &&
+        S.z0 == max(hz - 1, 0) && S.z1 == min(hz + 1, P.g.dz - 1)) {
+        const uint32_t e = __ldg(&bstart[home + 1]);
+        for (uint32_t k = __ldg(&bstart[home]); k < e; ++k) {
+            const uint32_t j = min(__ldg(&bcand[k]), nb - 1);
+            boundary_pair(xi, __ldg(&bpos[j]), P, bx, by, bz);
+        }
+    } else {
+        uint32_t c = 0;
+        boundary_sum<false, true>(xi, bpos, bcells, nb, P, bx, by, bz, c, __ldg(&bmask[home]), hx,
+                                  hy, hz);
+    }
+    bacc[i] = make_float4(bx, by, bz, 0.0f);
+}
+
 static __global__ void __launch_bounds__(256) boundary_force_kernel(
     const float4* __restrict__ pos, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint32_t* __restrict__ bmask,
@@ -129,24 +156,8 @@ static __global__ void __launch_bounds__(256) boundary_force_kernel(
         const int hz = cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz);
         const uint32_t home = linear_cell(P.g, hx, hy, hz);
         if (!list && !__ldg(&near_all[home])) continue;
-        float bx = 0.f, by = 0.f, bz = 0.f;
-        const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
-        const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&
-                            xi.z >= P.g.oz && xi.z < P.g.ez;
-        if (inside && S.x0 == max(hx - 1, 0) && S.x1 == min(hx + 1, P.g.dx - 1) &&
-            S.y0 == max(hy - 1, 0) && S.y1 == min(hy + 1, P.g.dy - 1) &&
-            S.z0 == max(hz - 1, 0) && S.z1 == min(hz + 1, P.g.dz - 1)) {
-            const uint32_t e = __ldg(&bstart[home + 1]);
-            for (uint32_t k = __ldg(&bstart[home]); k < e; ++k) {
-                const uint32_t j = min(__ldg(&bcand[k]), nb - 1);
-                boundary_pair(xi, __ldg(&bpos[j]), P, bx, by, bz);
-            }
-        } else {
-            uint32_t c = 0;
-            boundary_sum<false, true>(xi, bpos, bcells, nb, P, bx, by, bz, c, __ldg(&bmask[home]),
-                                      hx, hy, hz);
-        }
-        bacc[i] = make_float4(bx, by, bz, 0.0f);
+        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells, bmask, bstart, bcand, nb, P,
+                           bacc);
     }
 }
 
