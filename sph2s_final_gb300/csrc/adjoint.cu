@@ -280,7 +280,8 @@ int sph_rollout_backward(sph_solver* s, float* grad_v0, float* grad_x0, double* 
             adj_lambda_kernel<<<blocks, 256, 0, st>>>(r->gx, r->gv, n, r->dt, r->lam);
             adj_force_kernel<<<blocks, 256, 0, st>>>(
                 r->xh[k], r->vh[k], r->rho[k], r->aux[k], r->nbr[k], r->cnt[k], r->cells[k], s->bpos,
-                s->bcells, s->bnear, n, s->nb, s->P, r->mu, r->dt, r->lam, r->gx, r->gv, r->gx2,
+                s->bcells, s->bnear, s->bstart, s->bcand, n, s->nb, s->P, r->mu, r->dt, r->lam,
+                r->gx, r->gv, r->gx2,
                 r->gv2, r->grho, r->gmu_part);
             adj_sum_kernel<<<1, 32, 0, st>>>(r->gmu_part, blocks, r->gmu_acc);
             adj_density_kernel<<<blocks, 256, 0, st>>>(r->xh[k], r->nbr[k], r->cnt[k], r->cells[k],

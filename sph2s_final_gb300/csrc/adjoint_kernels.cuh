@@ -143,7 +143,8 @@ __device__ __forceinline__ float adj_force_one(
     const float* __restrict__ rho, const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
-    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, const SimParams& P, float mu,
+    const uint8_t* __restrict__ bnear, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, uint32_t n, uint32_t nb, const SimParams& P, float mu,
     float dt, const float4* __restrict__ lam, const float4* __restrict__ gx_in,
     const float4* __restrict__ gv_in, float4* __restrict__ gx_out, float4* __restrict__ gv_out,
     float* __restrict__ grho) {
@@ -168,51 +169,40 @@ __device__ __forceinline__ float adj_force_one(
         visit_force_neighbors(i, xi, pos, nbr4, nbr_count, cells, n, P, A);
         // boundary: b_i = sum_k beta(r) x_ik, beta = Bc shape(2r/h) / r^2
         float bx = 0.f, by = 0.f, bz = 0.f;
-        const uint32_t home = linear_cell(P.g, cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx),
-                                          cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy),
-                                          cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz));
+        const int hx = cell_coord(xi.x, P.g.ox, P.g.spacing, P.g.dx);
+        const int hy = cell_coord(xi.y, P.g.oy, P.g.spacing, P.g.dy);
+        const int hz = cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz);
+        const uint32_t home = linear_cell(P.g, hx, hy, hz);
         if (__ldg(&bnear[home])) {
-            const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
-            const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
-            for (int cz = s.z0; cz <= s.z1; ++cz)
-                for (int cy = s.y0; cy <= s.y1; ++cy) {
-                    const uint32_t row = linear_cell(P.g, 0, cy, cz);
-                    for (int cx = s.x0; cx <= s.x1; ++cx) {
-                        const uint2 r = __ldg(&bcells[row + cx]);
-                        const uint32_t e = min(r.y, nb);
-                        for (uint32_t k = r.x; k < e; ++k) {
-                            const float4 xk = __ldg(&bpos[k]);
-                            if (xk.w >= reach) break;  // the rest of the cell lies deeper
-                            float dx, dy, dz;
-                            const float r2 = dist2(xi.x, xi.y, xi.z, xk.x, xk.y, xk.z, dx, dy, dz);
-                            if (r2 < P.T) {
-                                const float rs = rsqrtf(r2);
-                                const float rr = r2 * rs;
-                                const float q = rr * P.two_over_h;
-                                float sh, shp;
-                                if (q < 2.0f / 3.0f) {
-                                    sh = 2.0f / 3.0f;
-                                    shp = 0.0f;
-                                } else if (q < 1.0f) {
-                                    sh = q * (2.0f - 1.5f * q);
-                                    shp = 2.0f - 3.0f * q;
-                                } else {
-                                    const float t2 = 2.0f - q;
-                                    sh = 0.5f * t2 * t2;
-                                    shp = -t2;
-                                }
-                                const float beta = P.bnd_coef * sh * rs * rs;
-                                const float betap = P.bnd_coef * (shp * P.two_over_h * rs * rs -
-                                                                  2.0f * sh * rs * rs * rs);
-                                const float rad = betap * rs *
-                                                  (A.li.x * dx + A.li.y * dy + A.li.z * dz);
-                                bx += beta * A.li.x + rad * dx;
-                                by += beta * A.li.y + rad * dy;
-                                bz += beta * A.li.z + rad * dz;
-                            }
-                        }
+            visit_boundary(xi, hx, hy, hz, home, bpos, bcells, bstart, bcand, nb, P,
+                           [&](const float4& xk) {
+                float dx, dy, dz;
+                const float r2 = dist2(xi.x, xi.y, xi.z, xk.x, xk.y, xk.z, dx, dy, dz);
+                if (r2 < P.T) {
+                    const float rs = rsqrtf(r2);
+                    const float rr = r2 * rs;
+                    const float q = rr * P.two_over_h;
+                    float sh, shp;
+                    if (q < 2.0f / 3.0f) {
+                        sh = 2.0f / 3.0f;
+                        shp = 0.0f;
+                    } else if (q < 1.0f) {
+                        sh = q * (2.0f - 1.5f * q);
+                        shp = 2.0f - 3.0f * q;
+                    } else {
+                        const float t2 = 2.0f - q;
+                        sh = 0.5f * t2 * t2;
+                        shp = -t2;
                     }
+                    const float beta = P.bnd_coef * sh * rs * rs;
+                    const float betap = P.bnd_coef * (shp * P.two_over_h * rs * rs -
+                                                      2.0f * sh * rs * rs * rs);
+                    const float rad = betap * rs * (A.li.x * dx + A.li.y * dy + A.li.z * dz);
+                    bx += beta * A.li.x + rad * dx;
+                    by += beta * A.li.y + rad * dy;
+                    bz += beta * A.li.z + rad * dz;
                 }
+            });
         }
         const float4 gxi = gx_in[i], gvi = gv_in[i];
         gx_out[i] = make_float4(gxi.x + A.gx + bx, gxi.y + A.gy + by, gxi.z + A.gz + bz, 0.f);
@@ -244,14 +234,16 @@ static __global__ void __launch_bounds__(256) adj_force_kernel(
     const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ nbr_count, const uint2* __restrict__ cells,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
-    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, SimParams P, float mu, float dt,
+    const uint8_t* __restrict__ bnear, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, uint32_t n, uint32_t nb, SimParams P, float mu, float dt,
     const float4* __restrict__ lam, const float4* __restrict__ gx_in,
     const float4* __restrict__ gv_in, float4* __restrict__ gx_out, float4* __restrict__ gv_out,
     float* __restrict__ grho, float* __restrict__ gmu_block) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float gmu_i = 0.0f;
     if (i < n)
-        gmu_i = adj_force_one(i, pos, vel, rho, aux, nbr4, nbr_count, cells, bpos, bcells, bnear, n,
+        gmu_i = adj_force_one(i, pos, vel, rho, aux, nbr4, nbr_count, cells, bpos, bcells, bnear,
+                              bstart, bcand, n,
                               nb, P, mu, dt, lam, gx_in, gv_in, gx_out, gv_out, grho);
     // per-block sum of d L / d mu (reduced in a fixed order afterwards)
     const float t = block_sum_fixed(gmu_i);

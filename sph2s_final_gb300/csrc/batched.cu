@@ -84,8 +84,8 @@ void enqueue_density(sph_batch* b) {
     cudaEventRecord(b->fork, b->stream);
     cudaStreamWaitEvent(b->side, b->fork, 0);
     b_boundary_force_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, b->side>>>(
-        b->tiles[1], b->ntiles[1], b->recs, b->spos, b->bpos, b->bcells, b->bnear, b->bmask,
-        b->bstart, b->bcand, b->NB, b->bacc);
+        b->tiles[1], b->ntiles[1], b->recs, b->spos, b->bpos, b->bcells, b->bnear, b->bstart,
+        b->bcand, b->NB, b->bacc);
     cudaEventRecord(b->join, b->side);
     switch (b->bs_density) {
         case 0: launch_density<128>(b, 0); break;
@@ -247,7 +247,6 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(dalloc(&b->cells, b->NC, b->owned));
     TRY(dalloc(&b->bcells, b->NC, b->owned));
     TRY(dalloc(&b->bnear, b->NC, b->owned));
-    TRY(dalloc(&b->bmask, b->NC, b->owned));
     TRY(dalloc(&b->bstart, (size_t)b->NC + 1, b->owned));
     TRY(dalloc(&b->bacc, b->N, b->owned));
     TRY(check_cuda(cudaMemset(b->bacc, 0, 16 * (size_t)std::max(b->N, 1u)), "memset", __FILE__, __LINE__));
@@ -345,17 +344,15 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
                                                                           reach, b->bnear + R.c_off);
         }
         TRY(check_cuda(cudaGetLastError(), "boundary flags", __FILE__, __LINE__));
-        // static boundary tables of every scene (boundary_tables.cuh): masks and
-        // candidate counts per scene, one prefix sum over all cells, then the
-        // candidates (global boundary indices)
+        // static boundary tables of every scene (boundary_tables.cuh): candidate
+        // counts per scene, one prefix sum over all cells, then the candidates
+        // (global boundary indices)
         std::vector<float> lims(num_scenes);
         for (uint32_t s = 0; s < num_scenes; ++s) {
             const SceneRec& R = b->recs_h[s];
             const uint32_t nc = sph_grid_num_cells(&scenes[s].config.grid);
             lims[s] = R.P.h * 1.01f + 4.0f * R.P.bmargin;
             if (!nc) continue;
-            boundary_mask_kernel<<<(nc + 255) / 256, 256, 0, b->stream>>>(b->bcells + R.c_off, R.P.g,
-                                                                          b->bmask + R.c_off);
             boundary_cand_kernel<false><<<(nc + 255) / 256, 256, 0, b->stream>>>(
                 b->bcells + R.c_off, b->bpos, b->bnear + R.c_off, R.P.g, b->NB, lims[s],
                 b->bstart + R.c_off, nullptr);

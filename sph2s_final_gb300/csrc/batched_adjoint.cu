@@ -67,7 +67,8 @@ static __global__ void __launch_bounds__(kTile) b_adj_force_kernel(
     const float* __restrict__ rho, const float2* __restrict__ aux, const uint4* __restrict__ nbr4,
     const uint32_t* __restrict__ cnt, const uint2* __restrict__ cells,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
-    const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb, float dt,
+    const uint8_t* __restrict__ bnear, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, uint32_t n, uint32_t nb, float dt,
     const float4* __restrict__ lam, const float4* __restrict__ gx_in,
     const float4* __restrict__ gv_in, float4* __restrict__ gx_out, float4* __restrict__ gv_out,
     float* __restrict__ grho, float* __restrict__ gmu_tile) {
@@ -79,7 +80,8 @@ static __global__ void __launch_bounds__(kTile) b_adj_force_kernel(
         if (i < R.p_off + R.p_n) {
             const SimParams P = R.P;
             g = adj_force_one(i, pos, vel, rho, aux, nbr4, cnt, cells + R.c_off, bpos,
-                              bcells + R.c_off, bnear + R.c_off, n, nb, P, mu_s[tile.x], dt, lam,
+                              bcells + R.c_off, bnear + R.c_off, bstart + R.c_off, bcand, n, nb,
+                              P, mu_s[tile.x], dt, lam,
                               gx_in, gv_in, gx_out, gv_out, grho);
         }
         const float s = block_sum_fixed(g);
@@ -401,7 +403,8 @@ int sphb_rollout_backward(sph_batch* b, float* grad_v0, float* grad_x0, double* 
             adj_lambda_kernel<<<blocks, kTile, 0, st>>>(r->gx, r->gv, N, r->dt, r->lam);
             b_adj_force_kernel<<<grid, kTile, 0, st>>>(
                 b->tiles[1], nt, b->recs, r->mu, r->xh[k], r->vh[k], r->rho[k], r->aux[k],
-                r->nbr[k], r->cnt[k], r->cells[k], b->bpos, b->bcells, b->bnear, N, b->NB, r->dt,
+                r->nbr[k], r->cnt[k], r->cells[k], b->bpos, b->bcells, b->bnear, b->bstart,
+                b->bcand, N, b->NB, r->dt,
                 r->lam, r->gx, r->gv, r->gx2, r->gv2, r->grho, r->gmu_part);
             b_adj_sum_kernel<<<(b->S + 127) / 128, 128, 0, st>>>(r->gmu_part, r->tfirst, r->tcount,
                                                                 b->S, r->gmu_acc);

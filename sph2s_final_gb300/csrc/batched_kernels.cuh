@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(BS) b_boundary_force_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
     const float4* __restrict__ pos, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear,
-    const uint32_t* __restrict__ bmask, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bstart,
     const uint32_t* __restrict__ bcand, uint32_t nb, float4* __restrict__ bacc) {
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(BS) b_boundary_force_kernel(
         const uint32_t home = linear_cell(g, hx, hy, hz);
         if (!__ldg(&bnear[R.c_off + home])) continue;
         const SimParams P = R.P;
-        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells + R.c_off, bmask + R.c_off,
-                           bstart + R.c_off, bcand, nb, P, bacc);
+        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells + R.c_off, bstart + R.c_off,
+                           bcand, nb, P, bacc);
     }
 }
 

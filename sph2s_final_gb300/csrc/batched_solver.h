@@ -33,7 +33,7 @@ struct sph_batch {
     uint32_t* vals[2] = {nullptr, nullptr};
     uint2 *cells = nullptr, *bcells = nullptr;
     uint8_t* bnear = nullptr;
-    uint32_t *bmask = nullptr, *bstart = nullptr, *bcand = nullptr;  // static boundary tables
+    uint32_t *bstart = nullptr, *bcand = nullptr;  // static boundary candidate tables
     float4* bacc = nullptr;              // the step's boundary force sums
     cudaStream_t side = nullptr;         // second branch of the step: the boundary force
     cudaEvent_t fork = nullptr, join = nullptr;

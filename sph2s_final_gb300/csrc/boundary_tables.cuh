@@ -1,6 +1,5 @@
 // boundary_tables.cuh -- the static tables of the boundary force pass
 // (boundary_force_kernel), built once per handle from the presorted boundary:
-// per cell, which of its 27 adjacent cells hold boundary particles (mask), and
 // per near-boundary cell the boundary particles of its cells +-1 within h plus
 // a margin of the cell's box, in the full scan's order (start, cand).
 #pragma once
@@ -10,7 +9,6 @@
 namespace sph {
 
 struct BoundaryTables {
-    uint32_t* mask = nullptr;   // per cell
     uint32_t* start = nullptr;  // per cell, plus the total at [ncells]
     uint32_t* cand = nullptr;   // boundary particle indices
 };
@@ -24,8 +22,7 @@ inline cudaError_t build_boundary_tables(const uint2* bcells, const float4* bpos
                                          uint32_t ncells, uint32_t nb, float h, float bmargin,
                                          cudaStream_t st, BoundaryTables& t) {
     const uint32_t blocks = (ncells + 255) / 256;
-    cudaError_t e = cudaMalloc(&t.mask, 4 * (size_t)(ncells ? ncells : 1));
-    if (e == cudaSuccess) e = cudaMalloc(&t.start, 4 * ((size_t)ncells + 1));
+    cudaError_t e = cudaMalloc(&t.start, 4 * ((size_t)ncells + 1));
     if (e != cudaSuccess) return e;
     const uint32_t words = (uint32_t)scan_scratch_words(ncells + 1);
     uint32_t* scratch = nullptr;
@@ -34,7 +31,6 @@ inline cudaError_t build_boundary_tables(const uint2* bcells, const float4* bpos
     uint32_t* total_d = scratch + words;
     const float lim = h * 1.01f + 4.0f * bmargin;  // any superset of the neighbours will do
     if (ncells) {
-        boundary_mask_kernel<<<blocks, 256, 0, st>>>(bcells, g, t.mask);
         boundary_cand_kernel<false><<<blocks, 256, 0, st>>>(bcells, bpos, bnear, g, nb, lim,
                                                             t.start, nullptr);
     }

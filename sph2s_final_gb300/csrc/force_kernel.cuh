@@ -60,34 +60,64 @@ __device__ __forceinline__ bool boundary_pair(const float4& xi, const float4& xj
 // Boundary force on a fluid particle at xi (computeBoundaryForceCell,
 // Solver.cu:300-344, scaled by m_b / (m + m_b)): every boundary particle of
 // the stencil within h, each cell's scan cut at the depth boundary_reach
-// allows; COUNT also counts them.  MASKED: `mask` has bit
-// (dz+1)*9 + (dy+1)*3 + (dx+1) set for each cell home + (dx, dy, dz) of the
-// grid that holds boundary particles, and stencil cells within one cell of
-// the home cell (hx, hy, hz) whose bit is clear are skipped (they hold none).
-template <bool COUNT, bool MASKED = false>
+// allows; COUNT also counts them.
+template <bool COUNT>
 __device__ __forceinline__ void boundary_sum(const float4& xi, const float4* __restrict__ bpos,
                                              const uint2* __restrict__ bcells, uint32_t nb,
                                              const SimParams& P, float& bx, float& by, float& bz,
-                                             uint32_t& bcnt, uint32_t mask = 0u, int hx = 0,
-                                             int hy = 0, int hz = 0) {
+                                             uint32_t& bcnt) {
     const Stencil s = stencil(P.g, xi.x, xi.y, xi.z, P.h);
     const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
     for (int cz = s.z0; cz <= s.z1; ++cz)
         for (int cy = s.y0; cy <= s.y1; ++cy) {
             const uint32_t row = linear_cell(P.g, 0, cy, cz);
             for (int cx = s.x0; cx <= s.x1; ++cx) {
-                if (MASKED) {
-                    const uint32_t ox = (uint32_t)(cx - hx + 1), oy = (uint32_t)(cy - hy + 1),
-                                   oz = (uint32_t)(cz - hz + 1);
-                    if (ox < 3u && oy < 3u && oz < 3u && !((mask >> (oz * 9u + oy * 3u + ox)) & 1u))
-                        continue;
-                }
                 const uint2 r = __ldg(&bcells[row + cx]);
                 const uint32_t e = min(r.y, nb);
                 for (uint32_t j = r.x; j < e; ++j) {
                     const float4 xj = __ldg(&bpos[j]);
                     if (xj.w >= reach) break;  // the rest of the cell lies deeper
                     if (boundary_pair(xi, xj, P, bx, by, bz) && COUNT) ++bcnt;
+                }
+            }
+        }
+}
+
+// Calls f(xk) for the boundary particles a particle at xi (home cell
+// (hx, hy, hz), linear `home`) must test, in the full scan's order: from the
+// home cell's static candidate list where it applies (inside the grid's box,
+// stencil = home +-1 clamped; see boundary_force_kernel), else from the
+// stencil scan cut by depth (boundary_reach).  A superset of the boundary
+// particles within h in both cases; f applies the r < h test itself.
+template <class F>
+__device__ __forceinline__ void visit_boundary(const float4& xi, int hx, int hy, int hz,
+                                               uint32_t home, const float4* __restrict__ bpos,
+                                               const uint2* __restrict__ bcells,
+                                               const uint32_t* __restrict__ bstart,
+                                               const uint32_t* __restrict__ bcand, uint32_t nb,
+                                               const SimParams& P, F&& f) {
+    const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
+    const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&
+                        xi.z >= P.g.oz && xi.z < P.g.ez;
+    if (bstart && inside && S.x0 == max(hx - 1, 0) && S.x1 == min(hx + 1, P.g.dx - 1) &&
+        S.y0 == max(hy - 1, 0) && S.y1 == min(hy + 1, P.g.dy - 1) &&
+        S.z0 == max(hz - 1, 0) && S.z1 == min(hz + 1, P.g.dz - 1)) {
+        const uint32_t e = __ldg(&bstart[home + 1]);
+        for (uint32_t k = __ldg(&bstart[home]); k < e; ++k)
+            f(__ldg(&bpos[min(__ldg(&bcand[k]), nb - 1)]));
+        return;
+    }
+    const float reach = boundary_reach(P.g, P.h, P.bmargin, xi.x, xi.y, xi.z);
+    for (int cz = S.z0; cz <= S.z1; ++cz)
+        for (int cy = S.y0; cy <= S.y1; ++cy) {
+            const uint32_t row = linear_cell(P.g, 0, cy, cz);
+            for (int cx = S.x0; cx <= S.x1; ++cx) {
+                const uint2 r = __ldg(&bcells[row + cx]);
+                const uint32_t e = min(r.y, nb);
+                for (uint32_t j = r.x; j < e; ++j) {
+                    const float4 xk = __ldg(&bpos[j]);
+                    if (xk.w >= reach) break;  // the rest of the cell lies deeper
+                    f(xk);
                 }
             }
         }
@@ -110,41 +140,24 @@ __device__ __forceinline__ uint32_t home_cell(const GridParams& g, const float4&
 // the boundary particles of those cells, in stencil order, that lie within
 // h plus a margin of the cell's box, a superset of every such particle's
 // boundary neighbours in the order of the full scan), whose loads do not
-// depend on one another; any other particle scans the stencil, skipping the
-// adjacent cells that hold no boundary particles (bmask).  Both give the
-// full scan's sum bit for bit.  boundary_force_one is the per-particle part
+// depend on one another; any other particle scans the stencil (visit_boundary).
+// Both give the full scan's sum bit for bit.  boundary_force_one is the per-particle part
 // (the batched step calls it per scene with that scene's tables).
 __device__ __forceinline__ void boundary_force_one(
     uint32_t i, const float4& xi, int hx, int hy, int hz, uint32_t home,
     const float4* __restrict__ bpos, const uint2* __restrict__ bcells,
-    const uint32_t* __restrict__ bmask, const uint32_t* __restrict__ bstart,
-    const uint32_t* __restrict__ bcand, uint32_t nb, const SimParams& P,
-    float4* __restrict__ bacc) {
+    const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcand, uint32_t nb,
+    const SimParams& P, float4* __restrict__ bacc) {
     float bx = 0.f, by = 0.f, bz = 0.f;
-    const Stencil S = stencil(P.g, xi.x, xi.y, xi.z, P.h);
-    const bool inside = xi.x >= P.g.ox && xi.x < P.g.ex && xi.y >= P.g.oy && xi.y < P.g.ey &&
-                        xi.z >= P.g.oz && xi.z < P.g.ez;
-    if (inside && S.x0 == max(hx - 1, 0) && S.x1 == min(hx + 1, P.g.dx - 1) &&
-        S.y0 == max(hy - 1, 0) && S.y1 == min(hy + 1, P.g.dy - 1) &&
-        S.z0 == max(hz - 1, 0) && S.z1 == min(hz + 1, P.g.dz - 1)) {
-        const uint32_t e = __ldg(&bstart[home + 1]);
-        for (uint32_t k = __ldg(&bstart[home]); k < e; ++k) {
-            const uint32_t j = min(__ldg(&bcand[k]), nb - 1);
-            boundary_pair(xi, __ldg(&bpos[j]), P, bx, by, bz);
-        }
-    } else {
-        uint32_t c = 0;
-        boundary_sum<false, true>(xi, bpos, bcells, nb, P, bx, by, bz, c, __ldg(&bmask[home]), hx,
-                                  hy, hz);
-    }
+    visit_boundary(xi, hx, hy, hz, home, bpos, bcells, bstart, bcand, nb, P,
+                   [&](const float4& xk) { boundary_pair(xi, xk, P, bx, by, bz); });
     bacc[i] = make_float4(bx, by, bz, 0.0f);
 }
 
 static __global__ void __launch_bounds__(256) boundary_force_kernel(
     const float4* __restrict__ pos, const float4* __restrict__ bpos,
-    const uint2* __restrict__ bcells, const uint32_t* __restrict__ bmask,
-    const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcand,
-    const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t n,
+    const uint2* __restrict__ bcells, const uint32_t* __restrict__ bstart,
+    const uint32_t* __restrict__ bcand, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t n,
     uint32_t nb, SimParams P, float4* __restrict__ bacc,
     const uint8_t* __restrict__ near_all = nullptr) {
     const uint32_t cnt = list ? min(*count, n) : n;
@@ -156,8 +169,7 @@ static __global__ void __launch_bounds__(256) boundary_force_kernel(
         const int hz = cell_coord(xi.z, P.g.oz, P.g.spacing, P.g.dz);
         const uint32_t home = linear_cell(P.g, hx, hy, hz);
         if (!list && !__ldg(&near_all[home])) continue;
-        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells, bmask, bstart, bcand, nb, P,
-                           bacc);
+        boundary_force_one(i, xi, hx, hy, hz, home, bpos, bcells, bstart, bcand, nb, P, bacc);
     }
 }
 

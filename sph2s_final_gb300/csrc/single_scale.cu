@@ -28,7 +28,7 @@ int free_solver(sph_solver* s) {
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->co_mem,  s->err,   s->stage, s->nbr, s->nbr_count,
-                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa, s->bacc, s->bmask, s->blist, s->bcount, s->bstart, s->bcand};
+                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa, s->bacc, s->blist, s->bcount, s->bstart, s->bcand};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->side) cudaStreamSynchronize(s->side);
@@ -100,9 +100,9 @@ void enqueue_density(sph_solver* s) {
     cudaEventRecord(s->fork, s->stream);
     cudaStreamWaitEvent(s->side, s->fork, 0);
     const uint32_t bgrid = std::min(blocks_for(s->n), (uint32_t)(2 * (s->sms > 0 ? s->sms : 1)));
-    boundary_force_kernel<<<bgrid, 256, 0, s->side>>>(s->spos, s->bpos, s->bcells, s->bmask,
-                                                      s->bstart, s->bcand, s->blist, s->bcount,
-                                                      s->n, s->nb, s->P, s->bacc);
+    boundary_force_kernel<<<bgrid, 256, 0, s->side>>>(s->spos, s->bpos, s->bcells, s->bstart,
+                                                      s->bcand, s->blist, s->bcount, s->n, s->nb,
+                                                      s->P, s->bacc);
     cudaEventRecord(s->join, s->side);
     density_kernel<false><<<blocks_for(s->n, kDensityThreads), kDensityThreads, 0, s->stream>>>(
         s->spos, s->cells, s->n, s->P, s->rho, s->aux, s->nbr, s->nbr_count, nullptr, s->xa,
@@ -314,7 +314,6 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
         BoundaryTables bt;
         const cudaError_t e = build_boundary_tables(s->bcells, s->bpos, s->bnear, s->P.g, s->ncells,
                                                     n_boundary, s->P.h, s->P.bmargin, s->stream, bt);
-        s->bmask = bt.mask;
         s->bstart = bt.start;
         s->bcand = bt.cand;
         TRY(check_cuda(e, "boundary tables", __FILE__, __LINE__));

@@ -174,29 +174,6 @@ static __global__ void __launch_bounds__(256) boundary_near_kernel(const uint2* 
     near[c] = f;
 }
 
-// Per cell, the adjacent cells (offsets -1..1 per axis, bit (dz+1)*9 +
-// (dy+1)*3 + (dx+1)) that lie in the grid and hold boundary particles.
-static __global__ void __launch_bounds__(256) boundary_mask_kernel(const uint2* __restrict__ bcells,
-                                                                   GridParams g,
-                                                                   uint32_t* __restrict__ mask) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nc = (uint32_t)g.dx * g.dy * g.dz;
-    if (c >= nc) return;
-    const int cx = (int)(c % (uint32_t)g.dx);
-    const int cy = (int)((c / (uint32_t)g.dx) % (uint32_t)g.dy);
-    const int cz = (int)(c / ((uint32_t)g.dx * g.dy));
-    uint32_t m = 0;
-    for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int x = cx + dx, y = cy + dy, z = cz + dz;
-                if (x < 0 || y < 0 || z < 0 || x >= g.dx || y >= g.dy || z >= g.dz) continue;
-                const uint2 r = bcells[linear_cell(g, x, y, z)];
-                if (r.x != kEmptyCell && r.x < r.y) m |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
-            }
-    mask[c] = m;
-}
-
 // Static boundary candidates of each cell flagged in `near`: the boundary
 // particles of the cells c +-1 (clamped), in stencil order (z, y, x, then the
 // cell's presorted order), whose distance to the cell's box is at most lim.

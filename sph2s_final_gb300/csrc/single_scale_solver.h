@@ -27,7 +27,6 @@ struct sph_solver {
     uint4* nbr = nullptr;           // neighbour lists, kMaxNbr per particle, [group][particle]
     uint32_t* nbr_count = nullptr;  // neighbours per particle (force set, r > 0)
     uint8_t* bnear = nullptr;       // per cell: boundary particles within stencil reach
-    uint32_t* bmask = nullptr;      // per cell: adjacent cells holding boundary particles (27 bits)
     uint32_t* bstart = nullptr;     // per cell + 1: start of its static boundary candidates ...
     uint32_t* bcand = nullptr;      // ... (boundary particle indices, boundary_cand_kernel)
     float4* bacc = nullptr;         // boundary force sums of near-boundary particles (step order)

@@ -104,7 +104,7 @@ int free_solver2(sph_solver2* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->side) cudaStreamSynchronize(s->side);
     for (void* p : s->owned) cudaFree(p);
-    for (void* p : {(void*)s->btab.mask, (void*)s->btab.start, (void*)s->btab.cand})
+    for (void* p : {(void*)s->btab.start, (void*)s->btab.cand})
         if (p) cudaFree(p);
     if (s->fork) cudaEventDestroy(s->fork);
     if (s->join) cudaEventDestroy(s->join);
@@ -254,8 +254,8 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         for (Pop* p : {&H, &L})
             if (p->n)
                 boundary_force_kernel<<<blocks_for(p->n), 256, 0, s->side>>>(
-                    p->spos, s->bpos, s->bcells, s->btab.mask, s->btab.start, s->btab.cand,
-                    nullptr, nullptr, p->n, s->nb, s->BP, p->bacc, s->bnear);
+                    p->spos, s->bpos, s->bcells, s->btab.start, s->btab.cand, nullptr, nullptr,
+                    p->n, s->nb, s->BP, p->bacc, s->bnear);
         cudaEventRecord(s->join, s->side);
     }
     if (H.n) {
