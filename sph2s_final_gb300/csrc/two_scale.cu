@@ -72,6 +72,8 @@ struct sph_solver2 {
     int sms = 0;
     cudaStream_t side = nullptr;  // second branch of the step: the boundary force
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t lowst = nullptr;  // the LOW density and force passes, beside the HIGH ones
+    cudaEvent_t pfork = nullptr, pjoin = nullptr;
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
     void* sort_mem = nullptr;
@@ -103,6 +105,10 @@ int free_solver2(sph_solver2* s) {
     if (!s) return SPH_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->side) cudaStreamSynchronize(s->side);
+    if (s->lowst) cudaStreamSynchronize(s->lowst);
+    if (s->pfork) cudaEventDestroy(s->pfork);
+    if (s->pjoin) cudaEventDestroy(s->pjoin);
+    if (s->lowst) cudaStreamDestroy(s->lowst);
     for (void* p : s->owned) cudaFree(p);
     for (void* p : {(void*)s->btab.start, (void*)s->btab.cand})
         if (p) cudaFree(p);
@@ -258,6 +264,15 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
                     p->n, s->nb, s->BP, p->bacc, s->bnear);
         cudaEventRecord(s->join, s->side);
     }
+    // The HIGH and LOW passes read only the step's sorted copies of both
+    // populations and write their own population's outputs (their shared
+    // group and step counters are integer atomics, whose sums do not depend
+    // on order), so the LOW passes run on a second stream beside the HIGH
+    // ones and fill the SMs the smaller population's waves leave idle;
+    // results are those of running them one after the other.
+    cudaStream_t lo = s->lowst;
+    cudaEventRecord(s->pfork, st);
+    cudaStreamWaitEvent(lo, s->pfork, 0);
     if (H.n) {
         if (debug && dbg_pop == 1)
             ts_density_kernel<1, true><<<blocks_for(H.n), 256, 0, st>>>(
@@ -270,14 +285,16 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
     }
     if (L.n) {
         if (debug && dbg_pop == 0)
-            ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
+            ts_density_kernel<0, true><<<blocks_for(L.n), 256, 0, lo>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, dnb_same, dnb_compl,
                 L.sgrp, gb, s->gsum, L.list, L.list_count, L.clist, L.clist_count);
         else
-            ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
+            ts_density_kernel<0, false><<<blocks_for(L.n), 256, 0, lo>>>(
                 L.spos, L.cells, L.n, H.spos, H.cells, H.n, s->P, L.rho, L.aux, nullptr, nullptr,
                 L.sgrp, gb, s->gsum, L.list, L.list_count, L.clist, L.clist_count);
     }
+    cudaEventRecord(s->pjoin, lo);
+    cudaStreamWaitEvent(st, s->pjoin, 0);
     // merge decisions (slab: start-of-step centroids; surface: this step's densities)
     if (gb && (s->P.axis >= 0 || s->P.surface))
         ts_group_decide_kernel<<<blocks_for(gb), 256, 0, st>>>(s->gsum, s->gready, gb, s->P.lo43,
@@ -286,6 +303,8 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
         cudaMemsetAsync(s->gmerge, 0, 4 * (size_t)gb, st);
     const uint32_t* gm = gb ? s->gmerge : nullptr;
     if (bsep) cudaStreamWaitEvent(st, s->join, 0);
+    cudaEventRecord(s->pfork, st);
+    cudaStreamWaitEvent(lo, s->pfork, 0);
     if (H.n) {
         TSOut o = outputs(H, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[1] : nullptr);
         if (debug && dbg_pop == 1)
@@ -300,14 +319,16 @@ void ts_front(sph_solver2* s, float dt, bool debug, int dbg_pop, uint32_t* dnb_s
     if (L.n) {
         TSOut o = outputs(L, dacc, dnb_bnd, (s->colour_on && !debug) ? s->colour[0] : nullptr);
         if (debug && dbg_pop == 0)
-            ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, st>>>(
+            ts_force_kernel<0, true><<<blocks_for(L.n), 256, 0, lo>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
                 H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o, nullptr);
         else
-            ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, st>>>(
+            ts_force_kernel<0, false><<<blocks_for(L.n), 256, 0, lo>>>(
                 L.spos, L.svel, L.sstt, L.sgrp, L.aux, L.cells, L.n, H.spos, H.svel, H.aux, H.cells,
                 H.n, s->bpos, s->bcells, s->bnear, s->nb, s->P, dt, gm, gb, s->gacc, s->ctl, L.rho, L.list, L.list_count, L.clist, L.clist_count, o, bsep ? L.bacc : nullptr);
     }
+    cudaEventRecord(s->pjoin, lo);
+    cudaStreamWaitEvent(st, s->pjoin, 0);
 }
 
 int check_err2(sph_solver2* s) {
@@ -438,6 +459,9 @@ int create_solver2(const sph_config2* config, const TSParams& P, uint64_t capL, 
     }
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
     TRY(check_cuda(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaStreamCreateWithFlags(&s->lowst, cudaStreamNonBlocking), "stream", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->pfork, cudaEventDisableTiming), "event", __FILE__, __LINE__));
+    TRY(check_cuda(cudaEventCreateWithFlags(&s->pjoin, cudaEventDisableTiming), "event", __FILE__, __LINE__));
     TRY(check_cuda(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming), "event", __FILE__, __LINE__));
     TRY(check_cuda(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming), "event", __FILE__, __LINE__));
     {
