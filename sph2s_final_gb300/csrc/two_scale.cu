@@ -368,7 +368,7 @@ int ts_step(sph_solver2* s, float dt) {
                 outputs(H, nullptr, nullptr), H.off, H.n, outputs(L, nullptr, nullptr), L.off,
                 L.soff, L.rho, L.n, s->P.mass[0], s->gmerge, s->moff, s->gacc, gb, s->ctl, hs, ls);
     }
-    ts_advance_counters_kernel<<<1, 1, 0, st>>>(s->ctl, s->cap_groups);
+    ts_advance_counters_kernel<<<1, 1, 0, st>>>(s->ctl, s->cap_groups, s->err);
     SPH_CUDA(cudaGetLastError());
     SPH_CUDA(cudaMemcpyAsync(s->ctl_host, s->ctl, 4 * kCtlWords, cudaMemcpyDeviceToHost, st));
     SPH_CUDA(cudaStreamSynchronize(st));
@@ -386,7 +386,8 @@ int ts_step(sph_solver2* s, float dt) {
     s->group_base = c[kCtlGroupBase];
     s->next_id[0] = c[kCtlPidL];
     s->next_id[1] = c[kCtlPidH];
-    return check_err2(s);
+    // the error word came back with the counts: no second round trip unless set
+    return c[kCtlErr] ? check_err2(s) : SPH_OK;
 }
 
 // Host copy of one population's persistent state, in the order the next

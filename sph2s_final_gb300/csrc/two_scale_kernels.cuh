@@ -62,6 +62,7 @@ enum TSCtl {
     kCtlFadedL,      // fade-in completions (atomic counters, cleared per step)
     kCtlFadedH,
     kCtlOverflow,    // capacity exceeded (HIGH, LOW or groups)
+    kCtlErr,         // the step's device error word, read back with the counts
     kCtlWords
 };
 
@@ -684,7 +685,9 @@ static __global__ void __launch_bounds__(256) ts_finish_kernel(
 
 // Advances the persistent counters after the step; the group count saturates
 // at the group capacity (the overflow was already reported).  One thread.
-static __global__ void ts_advance_counters_kernel(uint32_t* ctl, uint32_t cap_groups) {
+static __global__ void ts_advance_counters_kernel(uint32_t* ctl, uint32_t cap_groups,
+                                                  const uint32_t* err) {
+    ctl[kCtlErr] = *(volatile const uint32_t*)err;  // the last kernel of the step
     ctl[kCtlPidH] += 8u * ctl[kCtlSplits];
     ctl[kCtlPidL] += ctl[kCtlMerges];
     const uint64_t gb = (uint64_t)ctl[kCtlGroupBase] + ctl[kCtlSplits];
