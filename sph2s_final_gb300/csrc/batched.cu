@@ -83,7 +83,10 @@ void launch_force(sph_batch* b, int ti, float dt) {
 void enqueue_density(sph_batch* b) {
     cudaEventRecord(b->fork, b->stream);
     cudaStreamWaitEvent(b->side, b->fork, 0);
-    b_boundary_force_kernel<256><<<pgrid(b, b->ntiles[1]), 256, 0, b->side>>>(
+    // two blocks per SM: the density blocks fit beside them (a full persistent
+    // grid here would hold every SM until it drained, and density would wait)
+    b_boundary_force_kernel<256><<<std::min(pgrid(b, b->ntiles[1]), 2u * (uint32_t)b->sms), 256,
+                                   0, b->side>>>(
         b->tiles[1], b->ntiles[1], b->recs, b->spos, b->bpos, b->bcells, b->bnear, b->bstart,
         b->bcand, b->NB, b->bacc);
     cudaEventRecord(b->join, b->side);
