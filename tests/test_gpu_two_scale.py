@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from oracle.oracle_ts import TSRollout
+from sph2s_final_gb300._abi import SphError
 from sph2s_final_gb300 import scenes
 from sph2s_final_gb300.two_scale import HIGH, LOW, Solver2
 
@@ -74,6 +75,19 @@ def test_first_step_splits_the_slab(small):
         st = check_step(s, small)
         assert st["splits"] > 0
         assert s.counts()["high"] == 8 * st["splits"]
+
+
+def test_capacity_overflow_is_reported_and_the_device_stays_usable(small):
+    """A HIGH capacity below the first step's children: the step reports
+    SPH_E_CAPACITY (the device error word comes back with the step's counts),
+    the population is cut at its capacity (every write is checked against it),
+    and a fresh solver on the same device then steps as the oracle does."""
+    with Solver2(small.low, None, small.boundary, small.config, capacity_high=64) as s:
+        with pytest.raises(SphError, match="SPH_E_CAPACITY"):
+            s.advance(small.dt, 1)
+        assert s.counts()["high"] <= 64
+    with Solver2(small.low, None, small.boundary, small.config) as s:
+        assert check_step(s, small)["splits"] > 8
 
 
 def test_fading_and_removal_steps_match(small):
