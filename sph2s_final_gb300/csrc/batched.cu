@@ -75,7 +75,8 @@ template <int BS>
 void launch_force(sph_batch* b, int ti, float dt) {
     b_force_kernel<BS><<<pgrid(b, b->ntiles[ti]), BS, 0, b->stream>>>(
         b->tiles[ti], b->ntiles[ti], b->recs, b->spos, b->xa, b->svel, b->cells, b->nbr,
-        b->nbr_count, b->bpos, b->bcells, b->bnear, b->N, b->NB, dt, b->pos, b->vel, b->bacc);
+        b->nbr_count, b->bpos, b->bcells, b->bnear, b->N, b->NB, dt, b->pos, b->vel, b->bacc,
+        b->bflag);
 }
 
 // The density pass, and beside it on the second branch (fork / join events,
@@ -88,7 +89,7 @@ void enqueue_density(sph_batch* b) {
     b_boundary_force_kernel<256><<<std::min(pgrid(b, b->ntiles[1]), 2u * (uint32_t)b->sms), 256,
                                    0, b->side>>>(
         b->tiles[1], b->ntiles[1], b->recs, b->spos, b->bpos, b->bcells, b->bnear, b->bstart,
-        b->bcand, b->NB, b->bacc);
+        b->bcand, b->NB, b->bacc, b->bflag);
     cudaEventRecord(b->join, b->side);
     switch (b->bs_density) {
         case 0: launch_density<128>(b, 0); break;
@@ -128,7 +129,8 @@ int enqueue_neighborhood(sph_batch* b) {
     }
     b_gather_cells_kernel<256, true><<<pgrid(b, b->ntiles[1]), 256, 0, st>>>(
         b->tiles[1], b->ntiles[1], b->recs, b->keys[o], b->vals[o], b->N, b->shift, false, b->pos,
-        b->vel, b->spos, b->svel, b->cells, b->err, 0, b->coherent ? b->co.kprev : nullptr);
+        b->vel, b->spos, b->svel, b->cells, b->err, 0, b->coherent ? b->co.kprev : nullptr,
+        b->bnear, b->bflag);
     return o;
 }
 
@@ -252,6 +254,7 @@ int sphb_create(const sph_scene_desc* scenes, uint32_t num_scenes, sph_batch** o
     TRY(dalloc(&b->bnear, b->NC, b->owned));
     TRY(dalloc(&b->bstart, (size_t)b->NC + 1, b->owned));
     TRY(dalloc(&b->bacc, b->N, b->owned));
+    TRY(dalloc(&b->bflag, b->N, b->owned));
     TRY(check_cuda(cudaMemset(b->bacc, 0, 16 * (size_t)std::max(b->N, 1u)), "memset", __FILE__, __LINE__));
     TRY(dalloc(&b->bpos, b->NB, b->owned));
     TRY(check_cuda(cudaMalloc(&b->sort_mem, sort_scratch_bytes(nmax)), "sort scratch", __FILE__, __LINE__));

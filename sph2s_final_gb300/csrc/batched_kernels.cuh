@@ -90,13 +90,16 @@ __global__ void __launch_bounds__(BS) b_boundary_hash_hist_kernel(
 
 // Reorder + per-scene cell ranges; indices stored in the tables are global.
 // Keys are shifted right by key_shift first (the boundary presort's depth bits).
+// With bflag, also bflag[i] = bnear of particle i's cell (1 if boundary
+// particles lie within its stencil reach), for the boundary and force passes.
 template <int BS, bool WITH_VEL>
 __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
     const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ perm, uint32_t n,
     int shift, bool boundary, const float4* __restrict__ pos_in, const float4* __restrict__ vel_in,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint2* __restrict__ cells,
-    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr) {
+    uint32_t* __restrict__ err, int key_shift = 0, uint32_t* __restrict__ kprev_out = nullptr,
+    const uint8_t* __restrict__ bnear = nullptr, uint8_t* __restrict__ bflag = nullptr) {
     const uint32_t lmask = (1u << shift) - 1u;
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
@@ -117,6 +120,7 @@ __global__ void __launch_bounds__(BS) b_gather_cells_kernel(
         uint32_t* cw = reinterpret_cast<uint32_t*>(cells + R.c_off);
         const uint32_t c = (key >> shift) == tile.x ? morton_to_linear_checked(R.P.g, key & lmask)
                                                     : kEmptyCell;
+        if (bflag) bflag[i] = (c != kEmptyCell && __ldg(&bnear[R.c_off + c]) != 0) ? 1 : 0;
         if (c == kEmptyCell) {
             atomicOr(err, 2u);
             continue;
@@ -151,20 +155,22 @@ __global__ void __launch_bounds__(BS) b_density_kernel(
 }
 
 // Boundary force sums of the scenes' near-boundary particles (bnear of the
-// scene's cell), from the scenes' static candidate tables (boundary_force_one),
-// for b_force_kernel to load.
+// scene's cell, or bflag[i] where given), from the scenes' static candidate
+// tables (boundary_force_one), for b_force_kernel to load.
 template <int BS>
 __global__ void __launch_bounds__(BS) b_boundary_force_kernel(
     const uint2* __restrict__ tiles, uint32_t num_tiles, const SceneRec* __restrict__ recs,
     const float4* __restrict__ pos, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear,
     const uint32_t* __restrict__ bstart,
-    const uint32_t* __restrict__ bcand, uint32_t nb, float4* __restrict__ bacc) {
+    const uint32_t* __restrict__ bcand, uint32_t nb, float4* __restrict__ bacc,
+    const uint8_t* __restrict__ bflag = nullptr) {
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
         const SceneRec& R = recs[tile.x];
         const uint32_t i = tile.y + threadIdx.x;
         if (i >= R.p_off + R.p_n) continue;
+        if (bflag && !__ldg(&bflag[i])) continue;
         const float4 xi = pos[i];
         const GridParams& g = R.P.g;
         const int hx = cell_coord(xi.x, g.ox, g.spacing, g.dx);
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(BS) b_force_kernel(
     const uint32_t* __restrict__ nbr_count, const float4* __restrict__ bpos,
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-    const float4* __restrict__ bacc) {
+    const float4* __restrict__ bacc, const uint8_t* __restrict__ bflag = nullptr) {
     for (uint32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
         const uint2 tile = tiles[t];
         const SceneRec& R = recs[tile.x];
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__(BS) b_force_kernel(
         const SimParams P = R.P;
         force_one<0, true>(i, pos, xa, va, cells + R.c_off, nbr4, nbr_count, bpos,
                            bcells + R.c_off, bnear + R.c_off, n, nb, P, dt, pos_out, vel_out,
-                           nullptr, nullptr, bacc);
+                           nullptr, nullptr, bacc, bflag);
     }
 }
 

@@ -35,6 +35,7 @@ struct sph_batch {
     uint8_t* bnear = nullptr;
     uint32_t *bstart = nullptr, *bcand = nullptr;  // static boundary candidate tables
     float4* bacc = nullptr;              // the step's boundary force sums
+    uint8_t* bflag = nullptr;            // per sorted particle: bnear of its cell
     cudaStream_t side = nullptr;         // second branch of the step: the boundary force
     cudaEvent_t fork = nullptr, join = nullptr;
     float4* bpos = nullptr;

@@ -319,11 +319,11 @@ __global__ void __launch_bounds__(256) coherent_cells_kernel(const uint32_t* __r
     kprev[i] = (*(volatile const uint32_t*)err & 1u) ? 0xFFFFFFFFu : key;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
     const uint32_t c = morton_to_linear_checked(g, key);
+    near_append(near, c, i);
     if (c == kEmptyCell) {
         atomicOr(err, 2u);
         return;
     }
-    near_append(near, c, i);
     const uint32_t prev = i > 0 ? keys[i - 1] : 0u;
     if (i == 0 || prev != key) {
         cw[2 * c] = i;

@@ -174,18 +174,23 @@ __device__ __forceinline__ DepthClass depth_class(const GridParams& g, float x, 
 
 // Particles whose cell has boundary particles within stencil reach, listed
 // by the kernel that builds the step's cell ranges (sorted index, in no
-// particular order) for the step's boundary force pass.
+// particular order) for the step's boundary force pass; with `flag`, the same
+// fact per sorted particle (1 = listed), which the force pass reads in place
+// of recomputing the particle's cell and looking up bnear.
 struct NearList {
     const uint8_t* bnear = nullptr;  // per cell (static); nullptr: no list
     uint32_t* list = nullptr;        // capacity n
     uint32_t* count = nullptr;       // zeroed before the kernel
+    uint8_t* flag = nullptr;         // per sorted particle, or nullptr
 };
 
 // Appends sorted index i if its cell c is near the boundary: one atomic per
-// warp, each lane's slot from its rank among the appending lanes.
+// warp, each lane's slot from its rank among the appending lanes.  c may be
+// kEmptyCell (a key outside the grid after a failed sort): not listed.
 __device__ __forceinline__ void near_append(const NearList& L, uint32_t c, uint32_t i) {
     if (!L.list) return;
-    const bool want = L.bnear[c] != 0;
+    const bool want = c != kEmptyCell && L.bnear[c] != 0;
+    if (L.flag) L.flag[i] = want ? 1 : 0;
     const uint32_t am = __activemask();
     const uint32_t b = __ballot_sync(am, want);
     if (!b) return;

@@ -178,7 +178,10 @@ static __global__ void __launch_bounds__(256) boundary_force_kernel(
 // MODE 1 writes the acceleration and the boundary neighbour count instead.
 // Particle i of the sorted array; cells/bcells/bnear are the particle's own
 // grid tables (the batched solver passes per-scene tables and P).  BSEP: the
-// boundary sums were computed by boundary_force_kernel into bacc.
+// boundary sums were computed by boundary_force_kernel into bacc.  nflag: the
+// per-particle near-boundary flags written with the boundary pass's list
+// (NearList::flag); without it the particle's cell is recomputed and looked
+// up in bnear (the same answer: both test bnear of the particle's cell).
 template <int MODE, bool BSEP = false>
 __device__ __forceinline__ void force_one(
     uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ xa,
@@ -187,9 +190,10 @@ __device__ __forceinline__ void force_one(
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     const SimParams& P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
     float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b,
-    const float4* __restrict__ bacc = nullptr) {
+    const float4* __restrict__ bacc = nullptr, const uint8_t* __restrict__ nflag = nullptr) {
     const float4 xi = xa[i];  // (x, y, z, p/rho^2)
     const float4 vi = va[i];  // (v, 1/rho)
+    const bool listed = nflag && __ldg(&nflag[i]) != 0;
     const float tcoef = P.tens_coef * vi.w;
     ForceAcc A = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const uint32_t kc = nbr_count[i];
@@ -235,7 +239,7 @@ __device__ __forceinline__ void force_one(
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
     uint32_t bcnt = 0;
-    if (__ldg(&bnear[home_cell(P.g, xi)])) {
+    if (nflag ? listed : __ldg(&bnear[home_cell(P.g, xi)]) != 0) {
         if (BSEP) {
             const float4 b = bacc[i];
             bx = b.x;
@@ -270,11 +274,11 @@ __global__ void __launch_bounds__(256, 6) force_kernel(
     const uint2* __restrict__ bcells, const uint8_t* __restrict__ bnear, uint32_t n, uint32_t nb,
     SimParams P, float dt, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
     float* __restrict__ acc_out, uint32_t* __restrict__ nbr_b,
-    const float4* __restrict__ bacc = nullptr) {
+    const float4* __restrict__ bacc = nullptr, const uint8_t* __restrict__ nflag = nullptr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     force_one<MODE, BSEP>(i, pos, xa, va, cells, nbr4, nbr_count, bpos, bcells, bnear, n, nb, P,
-                          dt, pos_out, vel_out, acc_out, nbr_b, bacc);
+                          dt, pos_out, vel_out, acc_out, nbr_b, bacc, nflag);
 }
 
 }  // namespace sph

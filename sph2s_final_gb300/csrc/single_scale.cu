@@ -28,7 +28,7 @@ int free_solver(sph_solver* s) {
     void* ptrs[] = {s->pos,     s->vel,     s->spos,    s->svel,  s->rho,   s->aux,
                     s->keys[0], s->keys[1], s->vals[0], s->vals[1], s->cells, s->bcells,
                     s->bpos,    s->sort_mem, s->co_mem,  s->err,   s->stage, s->nbr, s->nbr_count,
-                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa, s->bacc, s->blist, s->bcount, s->bstart, s->bcand};
+                    s->bnear,   s->pos0, s->xacc, s->xall, s->xnb, s->xa, s->bacc, s->blist, s->bflag, s->bcount, s->bstart, s->bcand};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->side) cudaStreamSynchronize(s->side);
@@ -71,6 +71,7 @@ int enqueue_neighborhood(sph_solver* s) {
     near.bnear = s->bnear;
     near.list = s->blist;
     near.count = s->bcount;
+    near.flag = s->bflag;
     cudaMemsetAsync(s->bcount, 0, 4, st);
     if (!coherent || s->force_timeout) {
         const int passes = sort_passes(s->key_bits);
@@ -113,7 +114,7 @@ void enqueue_force(sph_solver* s, float dt) {
     cudaStreamWaitEvent(s->stream, s->join, 0);
     force_kernel<0, true><<<blocks_for(s->n), 256, 0, s->stream>>>(
         s->spos, s->xa, s->svel, s->cells, s->nbr, s->nbr_count, s->bpos, s->bcells, s->bnear,
-        s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr, s->bacc);
+        s->n, s->nb, s->P, dt, s->pos, s->vel, nullptr, nullptr, s->bacc, s->bflag);
 }
 
 // One step: Solver::Advance (Solver.cu:1082-1096) with integrate fused into
@@ -213,6 +214,7 @@ int create_solver(const sph_config* config, const HostInit& init, uint32_t n_flu
     TRY(dalloc(&s->bacc, n_fluid));
     TRY(check_cuda(cudaMemsetAsync(s->bacc, 0, sizeof(float4) * (n_fluid ? n_fluid : 1), s->stream), "memset", __FILE__, __LINE__));
     TRY(dalloc(&s->blist, n_fluid));
+    TRY(dalloc(&s->bflag, n_fluid));
     TRY(dalloc(&s->bcount, 1));
     {
         int dev = 0;

@@ -88,11 +88,11 @@ __global__ void __launch_bounds__(256) gather_cells_kernel(
     uint32_t key = keys_sorted[i] >> key_shift;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
     uint32_t c = morton_to_linear_checked(g, key);
+    near_append(near, c, i);
     if (c == kEmptyCell) {
         atomicOr(err, 2u);
         return;
     }
-    near_append(near, c, i);
     const uint32_t prev = i > 0 ? keys_sorted[i - 1] >> key_shift : 0u;
     if (i == 0 || prev != key) {
         cw[2 * c] = i;

@@ -32,6 +32,7 @@ struct sph_solver {
     float4* bacc = nullptr;         // boundary force sums of near-boundary particles (step order)
     uint32_t* blist = nullptr;      // the step's near-boundary particles (sorted indices) ...
     uint32_t* bcount = nullptr;     // ... and their number
+    uint8_t* bflag = nullptr;       // per sorted particle: 1 if in blist (read by the force pass)
     int sms = 0;                    // SM count (grid of the boundary force pass)
     cudaStream_t side = nullptr;    // second branch of the step: the boundary force
     cudaEvent_t fork = nullptr, join = nullptr;
