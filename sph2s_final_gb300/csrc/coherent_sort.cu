@@ -303,23 +303,46 @@ __global__ void __launch_bounds__(256) coherent_merge_kernel(
 
 // Cell ranges of the sorted keys (as gather_cells_kernel) and the keys
 // themselves as the next sort's kprev.
-__global__ void __launch_bounds__(256) coherent_cells_kernel(const uint32_t* __restrict__ keys,
-                                                             uint32_t n, GridParams g,
-                                                             uint2* __restrict__ cells,
-                                                             uint32_t* __restrict__ kprev,
-                                                             uint32_t* __restrict__ err,
-                                                             NearList near) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t key = keys[i];
+constexpr uint32_t kCellsThreads = 256;
+
+__global__ void __launch_bounds__(kCellsThreads) coherent_cells_kernel(
+    const uint32_t* __restrict__ keys, uint32_t n, GridParams g, uint2* __restrict__ cells,
+    uint32_t* __restrict__ kprev, uint32_t* __restrict__ err, NearList near) {
     // After a look-back timeout earlier in this sort (err bit 1, set only by
-    // previous kernels, so every thread sees the same value) the keys are not
+    // previous kernels, so every block sees the same value) the keys are not
     // sorted; 0xFFFFFFFF everywhere keeps kprev non-decreasing and makes every
-    // particle a mover in the next step, which then sorts from scratch.
-    kprev[i] = (*(volatile const uint32_t*)err & 1u) ? 0xFFFFFFFFu : key;
+    // particle a mover in the next step, which then sorts from scratch.  One
+    // thread per block reads the word: a read per thread put ~65,000 requests
+    // for one address on one L2 slice at 2M particles.
+    __shared__ uint32_t s_failed, s_base, s_warp[kCellsThreads / 32];
+    if (threadIdx.x == 0) s_failed = *(volatile const uint32_t*)err & 1u;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const uint32_t key = valid ? keys[i] : 0u;
+    if (valid) kprev[i] = s_failed ? 0xFFFFFFFFu : key;
     uint32_t* cw = reinterpret_cast<uint32_t*>(cells);
-    const uint32_t c = morton_to_linear_checked(g, key);
-    near_append(near, c, i);
+    const uint32_t c = valid ? morton_to_linear_checked(g, key) : kEmptyCell;
+    if (near.list) {  // near_append with one atomic per block instead of per warp
+        const bool want = c != kEmptyCell && near.bnear[c] != 0;
+        if (near.flag && valid) near.flag[i] = want ? 1 : 0;
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, want);
+        if (lane == 0) s_warp[warp] = __popc(b);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (uint32_t w = 0; w < kCellsThreads / 32; ++w) {
+                const uint32_t cnt = s_warp[w];
+                s_warp[w] = t;
+                t += cnt;
+            }
+            s_base = t ? atomicAdd(near.count, t) : 0u;
+        }
+        __syncthreads();
+        if (want) near.list[s_base + s_warp[warp] + __popc(b & ((1u << lane) - 1u))] = i;
+    }
+    if (!valid) return;
     if (c == kEmptyCell) {
         atomicOr(err, 2u);
         return;
@@ -410,8 +433,8 @@ void coherent_sort_cells(const CoherentSort& c, const float4* pos, const float4*
                  err, force_timeout, st);
     if (c.n == 0) return;
     cudaMemsetAsync(cells, 0xFF, sizeof(uint2) * (size_t)g.dx * g.dy * g.dz, st);
-    coherent_cells_kernel<<<(c.n + 255) / 256, 256, 0, st>>>(keys_out, c.n, g, cells, c.kprev,
-                                                              err, near);
+    coherent_cells_kernel<<<(c.n + kCellsThreads - 1) / kCellsThreads, kCellsThreads, 0, st>>>(
+        keys_out, c.n, g, cells, c.kprev, err, near);
 }
 
 void coherent_sort_keys(const CoherentSort& c, const uint32_t* keys, int key_bits,
