@@ -46,3 +46,20 @@ def test_config_states_whether_the_step_data_exceeds_l2():
     assert "fits in L2" in bench.config_for(d0, 1, small)["l2"]
     ours, d = bench.workload("c0")
     assert bench.config_for(d, 1, ours) == bench.config_for(d0, 1, small)
+
+
+def test_committed_ncu_figures_cover_the_single_scale_passes():
+    """The roofline block reads each pass's measured DRAM traffic and issue-active
+    share from the committed ncu summaries; every pass and workload it reports on
+    has both, and the traffic is at least the pass's algorithmic bytes (20 bytes
+    per particle + 8 per cell for density, 72 + 16 for force, at 2,097,152
+    particles in 128^3 cells and 512,000 in 80^3)."""
+    sizes = {"c1": (2097152, 128 ** 3), "c1m": (512000, 80 ** 3)}
+    per = {"density_kernel": (20, 8), "force_kernel": (72, 16)}
+    for wl, (n, cells) in sizes.items():
+        for kernel, (bp, bc) in per.items():
+            traffic = bench.committed_metric("traffic_bytes_per_launch", kernel, wl)
+            issue = bench.committed_metric("issue_active_pct", kernel, wl)
+            assert traffic is not None and issue is not None, (kernel, wl)
+            assert traffic >= bp * n + bc * cells, (kernel, wl, traffic)
+            assert 0.0 < issue <= 100.0
